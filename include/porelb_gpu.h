@@ -1,0 +1,203 @@
+/*
+ * porelb_gpu.h - C ABI of the GB300 sparse-lattice D3Q19 BGK solver.
+ *
+ * This is the drop-in boundary for porelb's hot path.  The reference has no
+ * plugin or FFI layer: its "interface" is the SIMULATION* function set of one
+ * C executable (porelb.h:127-165), the V.bin node table written by preprocess
+ * (preprocess.c:211-238) and the part_%03d_%07d.bin macro dumps
+ * (porelb.c:375-391).  Each entry point below names the reference function or
+ * file format it replaces.
+ *
+ * Conventions
+ *   - Every call returns an int status (PLB_OK == 0, negative on error); no
+ *     call exits the process.  The negative codes keep the reference's exit
+ *     codes where one exists (-6 density guard, porelb.c:338-342).
+ *   - Host buffers are caller-owned.  Device memory is owned by the handle.
+ *   - One CUDA stream per handle; a handle is not thread-safe.
+ *   - Nothing here takes a torch type; plain pointers and sizes only.
+ */
+#ifndef PORELB_GPU_H_
+#define PORELB_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLB_Q 19
+
+/* Neighbour entry, byte-compatible with NEIGHBOR_INFO (porelb.h:58-62):
+ * type@0, padding@1, pid@2, id@4; 8 bytes. */
+typedef struct {
+    uint8_t node_type;
+    uint8_t pad_;
+    uint16_t node_pid;
+    uint32_t node_id;
+} plb_neighbor_info;
+
+/* Fluid-node record, byte-compatible with NODE_INFO (porelb.h:73-76):
+ * x@0 y@2 z@4, padding@6, nb_info[18]@8; 152 bytes.  nb_info[i] describes
+ * the node at (x,y,z)+e[i+1], periodic (preprocess.c:183-196). */
+typedef struct {
+    uint16_t x, y, z;
+    uint16_t pad_;
+    plb_neighbor_info nb_info[PLB_Q - 1];
+} plb_node_info;
+
+/* enum NEIGHBOR_TYPE (porelb.h:55) */
+enum { PLB_TYPE_FLUID = 0, PLB_TYPE_SOLID = 1, PLB_TYPE_EXTERN = 2 };
+
+/* Status codes. */
+enum {
+    PLB_OK = 0,
+    PLB_ERR_ARG = -1,      /* bad argument / size */
+    PLB_ERR_IO = -2,       /* file open/read/write (porelb.c:18-22,65-69) */
+    PLB_ERR_TABLE = -3,    /* node table fails the check_V bounds test (porelb.c:115-141) */
+    PLB_ERR_CUDA = -4,     /* CUDA runtime error or no device */
+    PLB_ERR_NOMEM = -5,    /* host or device allocation failed */
+    PLB_ERR_DENSITY = -6,  /* density guard rho>1.2 | rho<0.5 (porelb.c:338-342) */
+    PLB_ERR_NUMP = -7,     /* num_p inconsistent with the table (porelb.c:29-34) */
+    PLB_ERR_STATE = -8     /* call out of order (e.g. step before init) */
+};
+
+/* Storage / arithmetic form of the distributions. */
+enum {
+    PLB_FP64_EXACT = 0, /* FP64 storage, reference operation order, no FMA: bit-exact */
+    PLB_FP64 = 1,       /* FP64 storage, FMA-contracted collision */
+    PLB_FP32 = 2,       /* FP32 storage, FP32 collision */
+    PLB_FP16DEV = 3,    /* scaled FP16 deviations f_i - w_i, FP32 collision */
+    PLB_BF16DEV = 4     /* scaled BF16 deviations f_i - w_i, FP32 collision */
+};
+
+/* Node ordering in device memory. */
+enum { PLB_ORDER_MORTON = 0, PLB_ORDER_REFERENCE = 1 };
+
+/* Halo semantics for tables written with num_p > 1. */
+enum {
+    PLB_HALO_AUTO = -1,        /* REMOTE_WINS when num_p > 1, else SINGLE */
+    PLB_HALO_SINGLE = 0,       /* one-rank run: last writer in node order wins */
+    PLB_HALO_REMOTE_WINS = 1   /* mpirun -np num_p: a cross-slab push overwrites
+                                  the local bounce-back write (porelb.c:430-433) */
+};
+
+typedef struct {
+    double tau;      /* relaxation time; reference hard-codes 0.8 (porelb.c:87) */
+    double force_x;  /* body force along x; reference hard-codes 1e-3 (porelb.c:91) */
+    int precision;   /* PLB_FP64_EXACT ... */
+    int ordering;    /* PLB_ORDER_MORTON or PLB_ORDER_REFERENCE */
+    int halo;        /* PLB_HALO_* */
+    int block_size;  /* threads per block for the step kernel; 0 = default */
+    int device;      /* CUDA device ordinal */
+    int reserved[7];
+} plb_params;
+
+typedef struct plb_sim plb_sim;
+
+/* ---------------------------------------------------------------- tables */
+
+/* Fill *p with the reference defaults: tau 0.8, force 1e-3 (init_para,
+ * porelb.c:83-94), FP64_EXACT, Morton order, automatic halo semantics. */
+void plb_default_params(plb_params *p);
+
+/* Replaces build_V (preprocess.c:74-209).  flag is nx*ny*nz uint8, x fastest,
+ * 1 = fluid, 0 = solid.  With out == NULL only *num_node is computed.
+ * v_sub_start receives num_p ints.  Requires nz % num_p == 0 (the reference
+ * writes out of bounds otherwise, preprocess.c:152).  Fields that the
+ * reference leaves defined are reproduced bit-exactly; SOLID entries carry the
+ * previous node's id/pid the way the reference's reused temporary does and
+ * padding bytes are zero. */
+int plb_build_table(const uint8_t *flag, int nx, int ny, int nz, int num_p,
+                    plb_node_info *out, int *num_node, int *v_sub_start);
+
+/* Replaces save_V (preprocess.c:211-238): header int32 num_node, num_p, nx,
+ * ny, nz; int32 v_sub_start[num_p]; NODE_INFO[num_node]. */
+int plb_write_vbin(const char *path, const plb_node_info *V, int num_node,
+                   int num_p, int nx, int ny, int nz, const int *v_sub_start);
+
+/* Replaces the V.bin reader of alloc_memory (porelb.c:15-81), for all ranks
+ * at once.  Read the header first, allocate, then read the body. */
+int plb_read_vbin_header(const char *path, int *num_node, int *num_p, int *nx,
+                         int *ny, int *nz);
+int plb_read_vbin(const char *path, plb_node_info *V, int *v_sub_start);
+
+/* Replaces check_V (porelb.c:115-141) with strict bounds (x < nx rather than
+ * the reference's x > nx test) and id checks on FLUID/EXTERN entries. */
+int plb_check_table(const plb_node_info *V, int num_node, int nx, int ny,
+                    int nz, int num_p, const int *v_sub_start);
+
+/* Deterministic periodic sphere pack (the geometry source of the benchmark
+ * configurations; the reference reads flag.bin from outside).  splitmix64
+ * stream from `seed`; each sphere draws centre x, y, z uniform in [0,n) and
+ * radius rmin + (rmax-rmin)*u; a cell (x,y,z) is solid iff its periodic
+ * minimum-image squared distance to a centre is <= R*R.  Spheres are added
+ * until the fluid fraction is <= porosity.  flag receives nx*ny*nz bytes. */
+int plb_sphere_pack(uint64_t seed, int nx, int ny, int nz, double rmin,
+                    double rmax, double porosity, uint8_t *flag,
+                    int *num_spheres, double *porosity_out);
+
+/* ---------------------------------------------------------------- solver */
+
+/* alloc_memory + check_V + init_para + build_send_recv_info
+ * (porelb.c:15-222): uploads the table, builds the pull table and the node
+ * permutation on the device, allocates the distributions.  V is num_node
+ * records in V.bin order (rank slabs concatenated in pid order). */
+int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
+               int num_p, const int *v_sub_start, const plb_params *p,
+               plb_sim **out);
+void plb_destroy(plb_sim *sim);
+
+/* init_dist_macro (porelb.c:224-238): rho=1, u=0, f0=f1=feq. */
+int plb_init_equilibrium(plb_sim *sim);
+
+/* nsteps iterations of the loop body of main (porelb.c:426-437): stream,
+ * halo (on-device), collide, with the half-force shift for it > 0
+ * (porelb.c:347-348).  Iterations are it_begin .. it_begin+nsteps-1.
+ * plb_step waits for the device and reports the density guard; the _async
+ * form only enqueues, and plb_sync waits and reports. */
+int plb_step(plb_sim *sim, int it_begin, int nsteps);
+int plb_step_async(plb_sim *sim, int it_begin, int nsteps);
+int plb_sync(plb_sim *sim);
+
+/* Rho, Ux, Uy, Uz of the last step, in reference node order (save_data,
+ * porelb.c:375-391).  Any pointer may be NULL. */
+int plb_get_macros(plb_sim *sim, double *rho, double *ux, double *uy,
+                   double *uz);
+
+/* save_data (porelb.c:375-391): writes part_%03d_%07d.bin for every rank of
+ * the table into dir (NULL = current directory), tagged `tag`. */
+int plb_save_parts(plb_sim *sim, const char *dir, int tag);
+
+/* Post-collision distributions f0 as reference AoS f[i*19+j], reference
+ * node order, converted to FP64 for the reduced-precision forms. */
+int plb_get_f(plb_sim *sim, double *f_aos);
+/* Overwrite the state from a reference-order AoS array. */
+int plb_set_f(plb_sim *sim, const double *f_aos);
+
+/* FP64 sums over the last step's macros: sum of Ux and of Rho. */
+int plb_reduce(plb_sim *sim, double *sum_ux, double *mass);
+
+/* Permeability k = <u_x> * nu / F.  k_darcy uses the superficial mean
+ * sum(Ux)/(nx*ny*nz); k_intrinsic uses sum(Ux)/num_node.  nu =(tau-1/2)/3
+ * (porelb.c:89).  Either pointer may be NULL. */
+int plb_permeability(plb_sim *sim, double *k_darcy, double *k_intrinsic);
+
+/* Details of the last density-guard trip: the iteration, node index in
+ * reference order, its coordinates and rho.  Returns PLB_OK if none. */
+int plb_last_error(plb_sim *sim, int *it, int *node, int *x, int *y, int *z,
+                   double *rho);
+
+/* Sizes and the handle's CUDA stream (a cudaStream_t). */
+int plb_info(plb_sim *sim, int *num_node, int *npad, int *precision,
+             size_t *device_bytes);
+void *plb_stream(plb_sim *sim);
+
+/* Human-readable text for a status code. */
+const char *plb_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PORELB_GPU_H_ */

@@ -1,0 +1,76 @@
+/*
+ * plb_internal.h - shared definitions of the CUDA translation units.
+ */
+#ifndef PLB_INTERNAL_H_
+#define PLB_INTERNAL_H_
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "porelb_gpu.h"
+
+namespace plb {
+
+constexpr int Q = 19;
+
+/* D3Q19 set in the reference order (porelb.h:10-50) as constexpr functions:
+ * inside fully unrolled loops they fold to immediates. */
+__host__ __device__ constexpr int ex(int j)
+{
+    return (j == 1 || j == 12 || j == 14 || j == 16 || j == 18) ? 1
+         : (j == 2 || j == 11 || j == 13 || j == 15 || j == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int ey(int j)
+{
+    return (j == 3 || j == 7 || j == 10 || j == 15 || j == 18) ? 1
+         : (j == 4 || j == 8 || j == 9 || j == 16 || j == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int ez(int j)
+{
+    return (j == 5 || j == 7 || j == 9 || j == 12 || j == 13) ? 1
+         : (j == 6 || j == 8 || j == 10 || j == 11 || j == 14) ? -1 : 0;
+}
+/* re[] (porelb.h:44-50): 1<->2, 3<->4, ... */
+__host__ __device__ constexpr int opp(int j)
+{
+    return j == 0 ? 0 : ((j & 1) ? j + 1 : j - 1);
+}
+/* weight class: 0 -> 1/3, 1 -> 1/18, 2 -> 1/36 */
+__host__ __device__ constexpr int wclass(int j)
+{
+    return j == 0 ? 0 : (j <= 6 ? 1 : 2);
+}
+
+/* A neighbour word: bit 31 set = bounce-back (read own node, direction
+ * re(j)); else bits 0..30 = source node of the pull.  Node index N (the
+ * "rest slot") holds the initial value of every direction and is never
+ * written: links no push or bounce ever writes read it. */
+constexpr uint32_t kBounce = 0x80000000u;
+constexpr uint32_t kSrcMask = 0x7fffffffu;
+
+struct StepArgs {
+    const void *fin;
+    void *fout;
+    const uint32_t *nbr;  /* [18][npad] */
+    const int *perm;      /* new -> reference index (density guard report) */
+    long long npad;
+    int n;
+    int it;
+    /* FP64 constants, computed on the host in the reference's order */
+    double omega, om1, k3, force, half_force;
+    /* FP32 forms */
+    float scale, inv_scale;
+    /* macros (rho, ux, uy, uz; stride npad) and per-block sums, or NULL */
+    double *macro;
+    double *partial;  /* [2][gridDim.x]: sum ux, sum rho */
+    unsigned long long *err; /* min over (it << 32 | reference index) */
+    unsigned int *flags;     /* bit 0: FP16 scale overflow */
+};
+
+/* Launch one step of the given precision. */
+cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
+                        int block, cudaStream_t s);
+
+}  // namespace plb
+
+#endif

@@ -1,0 +1,385 @@
+/*
+ * plb_step.cu - the fused pull-stream + BGK collide + body-force step.
+ *
+ * One thread per fluid node.  Thread i gathers its 19 post-stream values
+ * through the neighbour words (the on-device image of the reference's push
+ * stream, stream_inner_nodes porelb.c:285-300), relaxes them (collision,
+ * porelb.c:318-365) and writes its 19 post-collision values to the other
+ * ping-pong buffer.  Distributions are SoA, f[j][npad], so the 19 stores and
+ * the 18 neighbour-word loads of a warp are fully coalesced; the gathers hit
+ * nodes that the Morton order keeps close in memory.
+ *
+ * Forms:
+ *   FP64_EXACT  the reference's operations in the reference's order with
+ *               round-to-nearest intrinsics (no FMA contraction): bit-exact.
+ *   FP64        the same algebra restructured for FMA and one reciprocal.
+ *   FP32/FP16DEV/BF16DEV  relative deviations g = f/w - 1 stored (scaled)
+ *               in 32/16/16 bits, collision in FP32 on the deviations.
+ */
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "plb_internal.h"
+
+namespace plb {
+
+/* weights of the three classes, as the reference's doubles (porelb.h:36-42) */
+__device__ __forceinline__ double w64(int c)
+{
+    return c == 0 ? 1.0 / 3 : (c == 1 ? 1.0 / 18 : 1.0 / 36);
+}
+__device__ __forceinline__ float w32(int c)
+{
+    return c == 0 ? (float)(1.0 / 3) : (c == 1 ? (float)(1.0 / 18) : (float)(1.0 / 36));
+}
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+/* ------------------------------------------------------------- gather */
+
+template <typename T>
+__device__ __forceinline__ T ldg_t(const T *p) { return __ldg(p); }
+
+template <typename T>
+__device__ __forceinline__ void gather(const StepArgs &a, int i, T (&f)[Q])
+{
+    const T *fin = (const T *)a.fin;
+    const long long np = a.npad;
+    f[0] = ldg_t(fin + i);
+#pragma unroll
+    for (int j = 1; j < Q; j++) {
+        const uint32_t w = __ldcs(a.nbr + (long long)(j - 1) * np + i);
+        const T *p = (w & kBounce) ? fin + (long long)opp(j) * np + i
+                                   : fin + (long long)j * np + (w & kSrcMask);
+        f[j] = ldg_t(p);
+    }
+}
+
+/* ------------------------------------------------- FP64, reference order */
+
+/* e.u as the reference evaluates ((e0*u + e1*v) + e2*w) (porelb.c:9): terms
+ * with a zero coefficient add a signed zero, which changes no result. */
+template <int J>
+__device__ __forceinline__ double eu_ref(double u, double v, double w)
+{
+    double acc = 0.0;
+    bool first = true;
+    if (ex(J) != 0) { acc = ex(J) > 0 ? u : -u; first = false; }
+    if (ey(J) != 0) {
+        const double t = ey(J) > 0 ? v : -v;
+        acc = first ? t : dadd(acc, t);
+        first = false;
+    }
+    if (ez(J) != 0) {
+        const double t = ez(J) > 0 ? w : -w;
+        acc = first ? t : dadd(acc, t);
+        first = false;
+    }
+    return acc;
+}
+
+/* rho_u etc. accumulated in j order (porelb.c:330-336).  The first nonzero
+ * term is added to 0.0, which is exact. */
+template <int C>
+__device__ __forceinline__ double moment_ref(const double (&f)[Q])
+{
+    double acc = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int j = 0; j < Q; j++) {
+        const int e = C == 0 ? ex(j) : (C == 1 ? ey(j) : ez(j));
+        if (e == 0) continue;
+        if (first) {
+            acc = e > 0 ? f[j] : -f[j];
+            first = false;
+        } else {
+            acc = e > 0 ? dadd(acc, f[j]) : dsub(acc, f[j]);
+        }
+    }
+    return acc;
+}
+
+struct Macro {
+    double rho, u, v, w;
+    bool bad;
+};
+
+__device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
+                                                     const StepArgs &a)
+{
+    Macro m;
+    double rho = f[0];
+#pragma unroll
+    for (int j = 1; j < Q; j++) rho = dadd(rho, f[j]);
+    double ru = moment_ref<0>(f);
+    const double rv = moment_ref<1>(f);
+    const double rw = moment_ref<2>(f);
+    m.bad = (rho > 1.2) | (rho < 0.5);
+    if (a.it > 0) ru = dadd(ru, a.half_force);
+    const double u = __ddiv_rn(ru, rho);
+    const double v = __ddiv_rn(rv, rho);
+    const double w = __ddiv_rn(rw, rho);
+    m.rho = rho; m.u = u; m.v = v; m.w = w;
+
+    const double uv = dadd(dadd(dmul(u, u), dmul(v, v)), dmul(w, w));
+    const double uv15 = dmul(1.5, uv);
+    const double h0 = dmul(w64(0), rho);
+    const double h1 = dmul(w64(1), rho);
+    const double h2 = dmul(w64(2), rho);
+    /* omega + ((1-omega/2)*3*(e_x - u))*F for e_x = -1, 0, +1 */
+    const double am = dadd(a.omega, dmul(dmul(a.k3, dsub(-1.0, u)), a.force));
+    const double a0 = dadd(a.omega, dmul(dmul(a.k3, dsub(0.0, u)), a.force));
+    const double ap = dadd(a.omega, dmul(dmul(a.k3, dsub(1.0, u)), a.force));
+
+    /* rest direction: e.u = 0 gives ((1 + 0) + 0) - 1.5 uv */
+    {
+        const double feq = dmul(h0, dsub(1.0, uv15));
+        f[0] = dadd(dmul(a.om1, f[0]), dmul(a0, feq));
+    }
+    /* pairs (J, J+1) with e_{J+1} = -e_J: 3 e.u, 4.5 e.u and (4.5 e.u) e.u
+     * of the partner are exact negations / the same value. */
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        const int K = J + 1;
+        const double eu = (J == 1) ? eu_ref<1>(u, v, w)
+                        : (J == 3) ? eu_ref<3>(u, v, w)
+                        : (J == 5) ? eu_ref<5>(u, v, w)
+                        : (J == 7) ? eu_ref<7>(u, v, w)
+                        : (J == 9) ? eu_ref<9>(u, v, w)
+                        : (J == 11) ? eu_ref<11>(u, v, w)
+                        : (J == 13) ? eu_ref<13>(u, v, w)
+                        : (J == 15) ? eu_ref<15>(u, v, w)
+                                    : eu_ref<17>(u, v, w);
+        const double t3 = dmul(3.0, eu);
+        const double c2 = dmul(dmul(4.5, eu), eu);
+        const double h = wclass(J) == 1 ? h1 : h2;
+        const double feqJ = dmul(h, dsub(dadd(dadd(1.0, t3), c2), uv15));
+        const double feqK = dmul(h, dsub(dadd(dsub(1.0, t3), c2), uv15));
+        const double AJ = ex(J) > 0 ? ap : (ex(J) < 0 ? am : a0);
+        const double AK = ex(K) > 0 ? ap : (ex(K) < 0 ? am : a0);
+        f[J] = dadd(dmul(a.om1, f[J]), dmul(AJ, feqJ));
+        f[K] = dadd(dmul(a.om1, f[K]), dmul(AK, feqK));
+    }
+    return m;
+}
+
+/* ------------------------------------------------------ FP64 with FMA */
+
+__device__ __forceinline__ Macro collide_fp64_fma(double (&f)[Q],
+                                                   const StepArgs &a)
+{
+    Macro m;
+    double s[Q], d[Q];
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        s[J] = f[J] + f[J + 1];
+        d[J] = f[J] - f[J + 1];
+    }
+    double rho = f[0];
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) rho += s[J];
+    double jx = 0.0, jy = 0.0, jz = 0.0;
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        if (ex(J)) jx += ex(J) * d[J];
+        if (ey(J)) jy += ey(J) * d[J];
+        if (ez(J)) jz += ez(J) * d[J];
+    }
+    m.bad = (rho > 1.2) | (rho < 0.5);
+    if (a.it > 0) jx += a.half_force;
+    const double inv = 1.0 / rho;
+    const double u = jx * inv, v = jy * inv, w = jz * inv;
+    m.rho = rho; m.u = u; m.v = v; m.w = w;
+    const double uv15 = 1.5 * (u * u + v * v + w * w);
+    const double c = a.k3 * a.force;
+    const double am = a.omega - c * (1.0 + u);
+    const double a0 = a.omega - c * u;
+    const double ap = a.omega + c * (1.0 - u);
+    const double h0 = w64(0) * rho, h1 = w64(1) * rho, h2 = w64(2) * rho;
+    const double b1 = h1 - h1 * uv15, b2 = h2 - h2 * uv15;
+    f[0] = a.om1 * f[0] + a0 * (h0 - h0 * uv15);
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        const int K = J + 1;
+        const double eu = ex(J) * u + ey(J) * v + ez(J) * w;
+        const double h = wclass(J) == 1 ? h1 : h2;
+        const double b = wclass(J) == 1 ? b1 : b2;
+        const double sym = fma(4.5 * h * eu, eu, b);
+        const double anti = 3.0 * h * eu;
+        const double AJ = ex(J) > 0 ? ap : (ex(J) < 0 ? am : a0);
+        const double AK = ex(K) > 0 ? ap : (ex(K) < 0 ? am : a0);
+        f[J] = fma(a.om1, f[J], AJ * (sym + anti));
+        f[K] = fma(a.om1, f[K], AK * (sym - anti));
+    }
+    return m;
+}
+
+/* ----------------------------------------- FP32 collision on deviations */
+
+/* g_j = f_j / w_j - 1.  With rho = 1 + delta, the BGK + force update
+ *   f' = (1-omega) f + (omega + a_j) w rho (1 + P_j),
+ *   a_j = 3 (1 - omega/2) F (e_jx - u),  P_j = 3 e.u + 4.5 (e.u)^2 - 1.5 u.u
+ * becomes, exactly in real arithmetic,
+ *   g'_j = (1-omega) g_j + omega delta + rho ((omega + a_j) P_j + a_j),
+ * which keeps every FP32 quantity at deviation scale. */
+__device__ __forceinline__ Macro collide_dev32(float (&g)[Q], const StepArgs &a)
+{
+    Macro m;
+    float d[Q];
+#pragma unroll
+    for (int j = 0; j < Q; j++) d[j] = w32(wclass(j)) * g[j];
+    float s[Q], df[Q];
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        s[J] = d[J] + d[J + 1];
+        df[J] = d[J] - d[J + 1];
+    }
+    float delta = d[0];
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) delta += s[J];
+    float jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        if (ex(J)) jx += ex(J) * df[J];
+        if (ey(J)) jy += ey(J) * df[J];
+        if (ez(J)) jz += ez(J) * df[J];
+    }
+    const float rho = 1.0f + delta;
+    m.bad = (rho > 1.2f) | (rho < 0.5f);
+    if (a.it > 0) jx += (float)a.half_force;
+    const float inv = 1.0f / rho;
+    const float u = jx * inv, v = jy * inv, w = jz * inv;
+    m.rho = 1.0 + (double)delta;
+    m.u = u; m.v = v; m.w = w;
+    const float om = (float)a.omega, om1 = (float)a.om1;
+    const float c = (float)(a.k3 * a.force);
+    const float uv15 = 1.5f * (u * u + v * v + w * w);
+    const float base = om * delta;
+    const float am = -c * (1.0f + u), a0 = -c * u, ap = c * (1.0f - u);
+    {
+        const float P = -uv15;
+        g[0] = fmaf(om1, g[0], base + rho * fmaf(om + a0, P, a0));
+    }
+#pragma unroll
+    for (int J = 1; J < Q; J += 2) {
+        const int K = J + 1;
+        const float eu = ex(J) * u + ey(J) * v + ez(J) * w;
+        const float sym = fmaf(4.5f * eu, eu, -uv15);
+        const float PJ = fmaf(3.0f, eu, sym);
+        const float PK = fmaf(-3.0f, eu, sym);
+        const float aJ = ex(J) > 0 ? ap : (ex(J) < 0 ? am : a0);
+        const float aK = ex(K) > 0 ? ap : (ex(K) < 0 ? am : a0);
+        g[J] = fmaf(om1, g[J], base + rho * fmaf(om + aJ, PJ, aJ));
+        g[K] = fmaf(om1, g[K], base + rho * fmaf(om + aK, PK, aK));
+    }
+    return m;
+}
+
+/* storage conversion of the deviation forms */
+__device__ __forceinline__ float to_f(float x) { return x; }
+__device__ __forceinline__ float to_f(__half x) { return __half2float(x); }
+__device__ __forceinline__ float to_f(__nv_bfloat16 x) { return __bfloat162float(x); }
+template <typename T> __device__ __forceinline__ T from_f(float x);
+template <> __device__ __forceinline__ float from_f<float>(float x) { return x; }
+template <> __device__ __forceinline__ __half from_f<__half>(float x) { return __float2half_rn(x); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+
+/* --------------------------------------------------------------- kernel */
+
+template <int PREC> struct StoreOf { using T = double; };
+template <> struct StoreOf<PLB_FP32> { using T = float; };
+template <> struct StoreOf<PLB_FP16DEV> { using T = __half; };
+template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
+
+template <int PREC, bool MACRO>
+__global__ void __launch_bounds__(256)
+k_step(const StepArgs a)
+{
+    using T = typename StoreOf<PREC>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double sum_u = 0.0, sum_r = 0.0;
+    if (i < a.n) {
+        T raw[Q];
+        gather<T>(a, i, raw);
+        Macro m;
+        T *fout = (T *)a.fout;
+        const long long np = a.npad;
+        if constexpr (PREC == PLB_FP64_EXACT || PREC == PLB_FP64) {
+            if constexpr (PREC == PLB_FP64_EXACT) m = collide_fp64_exact(raw, a);
+            else m = collide_fp64_fma(raw, a);
+#pragma unroll
+            for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
+        } else {
+            float g[Q];
+#pragma unroll
+            for (int j = 0; j < Q; j++) g[j] = to_f(raw[j]) * a.inv_scale;
+            m = collide_dev32(g, a);
+            float big = 0.f;
+#pragma unroll
+            for (int j = 0; j < Q; j++) {
+                const float h = g[j] * a.scale;
+                big = fmaxf(big, fabsf(h));
+                fout[(long long)j * np + i] = from_f<T>(h);
+            }
+            if (PREC == PLB_FP16DEV && !(big <= 60000.f)) atomicOr(a.flags, 1u);
+        }
+        if (m.bad) {
+            const unsigned long long key =
+                ((unsigned long long)(unsigned)a.it << 32) | (unsigned)a.perm[i];
+            atomicMin(a.err, key);
+        }
+        if (MACRO) {
+            a.macro[i] = m.rho;
+            a.macro[np + i] = m.u;
+            a.macro[2 * np + i] = m.v;
+            a.macro[3 * np + i] = m.w;
+            sum_u = m.u;
+            sum_r = m.rho;
+        }
+    }
+    if (MACRO) {
+        __shared__ double su[32], sr[32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sum_u += __shfl_down_sync(0xffffffffu, sum_u, o);
+            sum_r += __shfl_down_sync(0xffffffffu, sum_r, o);
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) { su[wid] = sum_u; sr[wid] = sum_r; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tu = 0.0, tr = 0.0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); k++) { tu += su[k]; tr += sr[k]; }
+            a.partial[blockIdx.x] = tu;
+            a.partial[gridDim.x + blockIdx.x] = tr;
+        }
+    }
+}
+
+template <int PREC>
+static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
+                               cudaStream_t s)
+{
+    const int grid = (a.n + block - 1) / block;
+    if (grid == 0) return cudaSuccess;
+    if (macros) k_step<PREC, true><<<grid, block, 0, s>>>(a);
+    else k_step<PREC, false><<<grid, block, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
+                        int block, cudaStream_t s)
+{
+    switch (precision) {
+    case PLB_FP64_EXACT: return launch_prec<PLB_FP64_EXACT>(macros, a, block, s);
+    case PLB_FP64: return launch_prec<PLB_FP64>(macros, a, block, s);
+    case PLB_FP32: return launch_prec<PLB_FP32>(macros, a, block, s);
+    case PLB_FP16DEV: return launch_prec<PLB_FP16DEV>(macros, a, block, s);
+    case PLB_BF16DEV: return launch_prec<PLB_BF16DEV>(macros, a, block, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace plb

@@ -1,0 +1,202 @@
+"""Parity of the CUDA path with the reference (golden fixtures written by
+the compiled reference) and with the oracle, through the C ABI.
+
+Tolerances: FP64_EXACT is bit-exact (== on every double); FP64 (FMA form) is
+within 1e-12 relative on f and 1e-10 relative on the permeability."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+import porelb_gb300 as P
+from porelb_gb300 import _lib
+
+from helpers import golden_arrays, golden_meta, max_rel, noise_flag, pack_flag
+
+pytestmark = pytest.mark.gpu
+META = golden_meta()
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def gpu_run(V, dims, vs, tau, force, steps, precision="fp64_exact",
+            ordering="morton", halo="auto", chunks=None):
+    sim = P.Simulation(V, *dims, vs, tau=tau, force=force,
+                       precision=precision, ordering=ordering, halo=halo)
+    sim.init_dist_macro()
+    if chunks is None:
+        sim.step(steps)
+    else:
+        for c in chunks:
+            sim.step(c)
+    return sim
+
+
+@pytest.mark.parametrize("ordering", ["morton", "reference"])
+@pytest.mark.parametrize("name", ["noise_10x8x6_p1", "noise_8x6x8_p2",
+                                  "tiny_2x2x2_p1"])
+def test_exact_matches_golden(name, ordering):
+    m, g = META[name], golden_arrays(name)
+    V, vs = P.build_table(g["flag"], *m["dims"], m["num_p"])
+    with gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"],
+                 ordering=ordering) as sim:
+        assert (sim.get_f() == g["f0"]).all()
+        assert (sim.macros() == g["macros"]).all()
+
+
+def test_exact_c1_1000_steps_hash_and_dumps(tmp_path):
+    """64^3 sphere pack, seed 0, tau 1, F 1e-6, 1000 steps: f, macros and the
+    part files of the reference's dump schedule are the reference's bytes."""
+    m = META["c1_64_seed0"]
+    geo = m["geometry"]
+    flag = pack_flag(m["dims"], geo["seed"], geo["rmin"], geo["rmax"],
+                     geo["porosity"])
+    assert sha(flag) == geo["sha_flag"]
+    V, vs = P.build_table(flag, *m["dims"], 1)
+    sim = P.Simulation(V, *m["dims"], vs, tau=m["tau"], force=m["force"])
+    sim.init_dist_macro()
+    sim.step(1)
+    sim.save_data(str(tmp_path), tag=0)
+    sim.step(999)
+    sim.save_data(str(tmp_path), tag=1000)
+    assert sha(sim.get_f()) == m["sha_f0"]
+    assert sha(sim.macros()) == m["sha_macros"]
+    for fn, h in m["parts"].items():
+        with open(tmp_path / fn, "rb") as fh:
+            assert hashlib.sha256(fh.read()).hexdigest() == h, fn
+    kd, _ = sim.permeability()
+    assert abs(kd - m["k_darcy"]) <= 1e-10 * abs(m["k_darcy"])
+    su, mass = sim.reduce()
+    assert abs(mass - m["mass"]) <= 1e-12 * m["mass"]
+    sim.close()
+
+
+def test_exact_multirank_hash():
+    m = META["c1_64_seed0_p4_100"]
+    flag = pack_flag(m["dims"], 0, 6.0, 6.0, 0.40)
+    V, vs = P.build_table(flag, *m["dims"], m["num_p"])
+    with gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"]) as sim:
+        assert sha(sim.get_f()) == m["sha_f0"]
+        assert sha(sim.macros()) == m["sha_macros"]
+
+
+CASES = [((7, 9, 6), 0.2, 1, 1), ((8, 8, 8), 0.5, 2, 2), ((5, 3, 12), 0.4, 3, 4),
+         ((3, 3, 3), 0.0, 4, 1), ((1, 1, 2), 0.0, 5, 1), ((2, 2, 2), 0.3, 6, 1),
+         ((13, 1, 17), 0.3, 7, 1), ((33, 17, 9), 0.45, 8, 3)]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_exact_matches_oracle_on_noise(case):
+    dims, p_solid, seed, num_p = case
+    flag = noise_flag(dims, p_solid, seed)
+    V, vs = P.build_table(flag, *dims, num_p)
+    s = O.OracleSim(V, *dims, vs, 0.7, 3e-3)
+    s.init()
+    assert s.run(15, threads=num_p)[0] == 0
+    with gpu_run(V, dims, vs, 0.7, 3e-3, 15) as sim:
+        assert (sim.get_f() == s.f0()).all()
+        assert (sim.macros() == s.macros()).all()
+
+
+def test_single_rank_semantics_on_multirank_table():
+    """halo='single' on a 3-slab table gives the one-rank result."""
+    dims = (10, 8, 9)
+    flag = noise_flag(dims, 0.35, 12)
+    V1, vs1 = P.build_table(flag, *dims, 1)
+    V3, vs3 = P.build_table(flag, *dims, 3)
+    with gpu_run(V1, dims, vs1, 0.9, 1e-3, 20) as a, \
+            gpu_run(V3, dims, vs3, 0.9, 1e-3, 20, halo="single") as b:
+        assert (a.get_f() == b.get_f()).all()
+
+
+def test_chunked_steps_equal_one_call():
+    dims = (12, 10, 8)
+    flag = noise_flag(dims, 0.3, 13)
+    V, vs = P.build_table(flag, *dims, 1)
+    with gpu_run(V, dims, vs, 0.8, 1e-3, 17) as a, \
+            gpu_run(V, dims, vs, 0.8, 1e-3, 17, chunks=[1, 5, 11]) as b:
+        assert (a.get_f() == b.get_f()).all()
+        assert (a.macros() == b.macros()).all()
+
+
+def test_fp64_fma_within_1e12_of_reference_c1():
+    m = META["c1_64_seed0"]
+    flag = pack_flag(m["dims"], 0, 6.0, 6.0, 0.40)
+    V, vs = P.build_table(flag, *m["dims"], 1)
+    ref = gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"])
+    fma = gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"],
+                  precision="fp64")
+    assert sha(ref.get_f()) == m["sha_f0"]
+    assert max_rel(fma.get_f(), ref.get_f()) <= 1e-12
+    kd = fma.permeability()[0]
+    assert abs(kd - m["k_darcy"]) <= 1e-10 * abs(m["k_darcy"])
+    ref.close()
+    fma.close()
+
+
+def test_set_get_roundtrip_and_restart():
+    dims = (9, 8, 7)
+    flag = noise_flag(dims, 0.3, 14)
+    V, vs = P.build_table(flag, *dims, 1)
+    with gpu_run(V, dims, vs, 0.8, 1e-3, 10) as a, \
+            gpu_run(V, dims, vs, 0.8, 1e-3, 0) as b:
+        f = a.get_f()
+        b.set_f(f)
+        assert (b.get_f() == f).all()
+        a.step(5)
+        b.step(5, it_begin=10)
+        assert (a.get_f() == b.get_f()).all()
+
+
+def test_density_guard_matches_oracle():
+    dims = (8, 8, 8)
+    flag = noise_flag(dims, 0.3, 21)
+    V, vs = P.build_table(flag, *dims, 1)
+    s = O.OracleSim(V, *dims, vs, 0.505, 0.2)
+    s.init()
+    st, bad_it, bad_node = s.run(500)
+    assert st == -6
+    sim = P.Simulation(V, *dims, vs, tau=0.505, force=0.2)
+    sim.init_dist_macro()
+    with pytest.raises(P.PorelbError) as e:
+        sim.step(500)
+    assert e.value.status == _lib.ERR_DENSITY
+    err = sim.last_error()
+    assert err["it"] == bad_it and err["node"] == bad_node
+    assert (err["x"], err["y"], err["z"]) == (int(V["x"][bad_node]),
+                                             int(V["y"][bad_node]),
+                                             int(V["z"][bad_node]))
+    sim.close()
+
+
+def test_rejects_bad_tables_and_order():
+    dims = (6, 5, 4)
+    flag = noise_flag(dims, 0.25, 15)
+    V, vs = P.build_table(flag, *dims, 1)
+    bad = V.copy()
+    k = np.argwhere(bad["nb_info"]["node_type"][0] == 0)[0, 0]
+    bad["nb_info"]["node_id"][0, k] = len(V) + 5
+    with pytest.raises(P.PorelbError) as e:
+        P.Simulation(bad, *dims, vs)
+    assert e.value.status == _lib.ERR_TABLE
+    dup = V.copy()
+    dup["x"][1], dup["y"][1], dup["z"][1] = dup["x"][0], dup["y"][0], dup["z"][0]
+    with pytest.raises(P.PorelbError) as e:
+        P.Simulation(dup, *dims, vs)
+    assert e.value.status == _lib.ERR_TABLE
+    sim = P.Simulation(V, *dims, vs)
+    with pytest.raises(P.PorelbError) as e:
+        sim.step(1)
+    assert e.value.status == _lib.ERR_STATE
+    sim.close()
+
+
+def test_empty_domain():
+    V, vs = P.build_table(np.zeros(8, np.uint8), 2, 2, 2)
+    with gpu_run(V, (2, 2, 2), vs, 0.8, 1e-3, 3) as sim:
+        assert sim.get_f().size == 0
+        assert sim.reduce() == (0.0, 0.0)
