@@ -31,7 +31,7 @@ FALLBACK_HBM = 6800.0
 
 # algorithmic bytes per fluid-node update: 19 loads + 19 stores of the
 # distribution + 18 int32 neighbour words
-BYTES_PER_NODE = {"fp64_exact": 376, "fp64": 376, "fp32": 224,
+BYTES_PER_NODE = {"fp64_exact": 376, "fp64": 376, "fp64_fma": 376, "fp32": 224,
                   "fp16dev": 148, "bf16dev": 148}
 
 WORKLOADS = {

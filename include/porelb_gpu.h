@@ -65,10 +65,12 @@ enum {
 /* Storage / arithmetic form of the distributions. */
 enum {
     PLB_FP64_EXACT = 0, /* FP64 storage, reference operation order, no FMA: bit-exact */
-    PLB_FP64 = 1,       /* FP64 storage, FMA-contracted collision */
+    PLB_FP64 = 1,       /* FP64 storage, collision in exact Q60 fixed point on
+                           the integer pipes (within 1e-12 of the reference) */
     PLB_FP32 = 2,       /* FP32 storage, FP32 collision */
     PLB_FP16DEV = 3,    /* scaled FP16 deviations f_i - w_i, FP32 collision */
-    PLB_BF16DEV = 4     /* scaled BF16 deviations f_i - w_i, FP32 collision */
+    PLB_BF16DEV = 4,    /* scaled BF16 deviations f_i - w_i, FP32 collision */
+    PLB_FP64_FMA = 5    /* FP64 storage, FMA-contracted FP64 collision */
 };
 
 /* Node ordering in device memory. */

@@ -27,7 +27,7 @@ OK = 0
 ERR_ARG, ERR_IO, ERR_TABLE, ERR_CUDA = -1, -2, -3, -4
 ERR_NOMEM, ERR_DENSITY, ERR_NUMP, ERR_STATE = -5, -6, -7, -8
 
-FP64_EXACT, FP64, FP32, FP16DEV, BF16DEV = 0, 1, 2, 3, 4
+FP64_EXACT, FP64, FP32, FP16DEV, BF16DEV, FP64_FMA = 0, 1, 2, 3, 4, 5
 ORDER_MORTON, ORDER_REFERENCE = 0, 1
 HALO_AUTO, HALO_SINGLE, HALO_REMOTE_WINS = -1, 0, 1
 

@@ -19,7 +19,7 @@ from ._lib import NODE_DTYPE, Q
 
 PRECISIONS = {"fp64_exact": _lib.FP64_EXACT, "fp64": _lib.FP64,
               "fp32": _lib.FP32, "fp16dev": _lib.FP16DEV,
-              "bf16dev": _lib.BF16DEV}
+              "bf16dev": _lib.BF16DEV, "fp64_fma": _lib.FP64_FMA}
 ORDERINGS = {"morton": _lib.ORDER_MORTON, "reference": _lib.ORDER_REFERENCE}
 HALOS = {"auto": _lib.HALO_AUTO, "single": _lib.HALO_SINGLE,
          "remote_wins": _lib.HALO_REMOTE_WINS}

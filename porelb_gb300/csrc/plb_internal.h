@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "porelb_gpu.h"
+#include "plb_fx.h"
 
 namespace plb {
 
@@ -58,8 +59,11 @@ struct StepArgs {
     int it;
     /* FP64 constants, computed on the host in the reference's order */
     double omega, om1, k3, force, half_force;
-    /* FP32 forms */
+    /* FP32 forms (host-rounded from the FP64 constants) */
     float scale, inv_scale;
+    float omega_f, om1_f, c_f, half_force_f;
+    /* fixed-point form */
+    fx::Consts fxk;
     /* macros (rho, ux, uy, uz; stride npad) and per-block sums, or NULL */
     double *macro;
     double *partial;  /* [2][gridDim.x]: sum ux, sum rho */

@@ -43,10 +43,12 @@ struct plb_sim {
     unsigned int *flags;
     int *v_sub_start; /* host, num_p + 1 */
     double tau, omega, om1, k3, force, half_force, nu;
+    fx::Consts fxk;
     float scale;
     int initialized, macro_valid;
     size_t dev_bytes;
     int err_it, err_node;
+    int fallback_nodes_seen;
 };
 
 #define CK(call)                                                          \
@@ -453,7 +455,8 @@ static size_t elem_size(int precision)
 {
     switch (precision) {
     case PLB_FP64_EXACT:
-    case PLB_FP64: return 8;
+    case PLB_FP64:
+    case PLB_FP64_FMA: return 8;
     case PLB_FP32: return 4;
     case PLB_FP16DEV:
     case PLB_BF16DEV: return 2;
@@ -625,6 +628,7 @@ int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
     s->force = p->force_x;
     plb_host_constants(p->tau, p->force_x, &s->omega, &s->om1, &s->k3,
                        &s->half_force, &s->nu);
+    s->fxk = fx::make_consts(p->tau, p->force_x);
     s->scale = p->precision == PLB_FP16DEV ? 1024.0f : 1.0f;
     s->v_sub_start = (int *)malloc(sizeof(int) * (size_t)(num_p + 1));
     if (!s->v_sub_start) { free(s); return PLB_ERR_NOMEM; }
@@ -675,6 +679,7 @@ int plb_init_equilibrium(plb_sim *s)
     switch (s->precision) {
     case PLB_FP64_EXACT:
     case PLB_FP64:
+    case PLB_FP64_FMA:
         k_init_fp64<<<g, 256, 0, s->stream>>>((double *)s->f[0], (double *)s->f[1], s->npad, s->n);
         break;
     case PLB_FP32:
@@ -720,6 +725,11 @@ int plb_step_async(plb_sim *s, int it_begin, int nsteps)
     a.half_force = s->half_force;
     a.scale = s->scale;
     a.inv_scale = 1.0f / s->scale;
+    a.omega_f = (float)s->omega;
+    a.om1_f = (float)s->om1;
+    a.c_f = (float)(s->k3 * s->force);
+    a.half_force_f = (float)s->half_force;
+    a.fxk = s->fxk;
     a.macro = s->macro;
     a.partial = s->partial;
     a.err = s->err;
@@ -754,6 +764,7 @@ int plb_sync(plb_sim *s)
         s->err_node = (int)(key & 0xffffffffu);
         return PLB_ERR_DENSITY;
     }
+    if (flags & 2u) s->fallback_nodes_seen = 1;
     if (flags & 1u) {
         fprintf(stderr, "porelb_gpu: FP16 deviation overflow; lower the scale\n");
         return PLB_ERR_STATE;
@@ -827,7 +838,8 @@ int plb_get_f(plb_sim *s, double *f_aos)
     const void *f = s->f[s->cur];
     switch (s->precision) {
     case PLB_FP64_EXACT:
-    case PLB_FP64: k_get_f_fp64<<<g, 256, 0, s->stream>>>((const double *)f, s->perm, s->npad, s->n, d); break;
+    case PLB_FP64:
+    case PLB_FP64_FMA: k_get_f_fp64<<<g, 256, 0, s->stream>>>((const double *)f, s->perm, s->npad, s->n, d); break;
     case PLB_FP32: k_get_f_dev<float><<<g, 256, 0, s->stream>>>((const float *)f, s->perm, s->npad, s->n, 1.0f / s->scale, d); break;
     case PLB_FP16DEV: k_get_f_dev<__half><<<g, 256, 0, s->stream>>>((const __half *)f, s->perm, s->npad, s->n, 1.0f / s->scale, d); break;
     default: k_get_f_dev<__nv_bfloat16><<<g, 256, 0, s->stream>>>((const __nv_bfloat16 *)f, s->perm, s->npad, s->n, 1.0f / s->scale, d); break;
@@ -858,7 +870,8 @@ int plb_set_f(plb_sim *s, const double *f_aos)
     if (e == cudaSuccess) {
         switch (s->precision) {
         case PLB_FP64_EXACT:
-        case PLB_FP64: k_set_f_fp64<<<g, 256, 0, s->stream>>>((double *)f, s->perm, s->npad, s->n, d); break;
+        case PLB_FP64:
+        case PLB_FP64_FMA: k_set_f_fp64<<<g, 256, 0, s->stream>>>((double *)f, s->perm, s->npad, s->n, d); break;
         case PLB_FP32: k_set_f_dev<float><<<g, 256, 0, s->stream>>>((float *)f, s->perm, s->npad, s->n, s->scale, d); break;
         case PLB_FP16DEV: k_set_f_dev<__half><<<g, 256, 0, s->stream>>>((__half *)f, s->perm, s->npad, s->n, s->scale, d); break;
         default: k_set_f_dev<__nv_bfloat16><<<g, 256, 0, s->stream>>>((__nv_bfloat16 *)f, s->perm, s->npad, s->n, s->scale, d); break;

@@ -12,7 +12,9 @@
  * Forms:
  *   FP64_EXACT  the reference's operations in the reference's order with
  *               round-to-nearest intrinsics (no FMA contraction): bit-exact.
- *   FP64        the same algebra restructured for FMA and one reciprocal.
+ *   FP64        exact Q60 fixed-point collision on the integer pipes
+ *               (plb_fx.h); nodes outside its range fall back to FP64_FMA.
+ *   FP64_FMA    the same algebra in native FP64, restructured for FMA.
  *   FP32/FP16DEV/BF16DEV  relative deviations g = f/w - 1 stored (scaled)
  *               in 32/16/16 bits, collision in FP32 on the deviations.
  */
@@ -248,13 +250,13 @@ __device__ __forceinline__ Macro collide_dev32(float (&g)[Q], const StepArgs &a)
     }
     const float rho = 1.0f + delta;
     m.bad = (rho > 1.2f) | (rho < 0.5f);
-    if (a.it > 0) jx += (float)a.half_force;
+    if (a.it > 0) jx += a.half_force_f;
     const float inv = 1.0f / rho;
     const float u = jx * inv, v = jy * inv, w = jz * inv;
     m.rho = 1.0 + (double)delta;
     m.u = u; m.v = v; m.w = w;
-    const float om = (float)a.omega, om1 = (float)a.om1;
-    const float c = (float)(a.k3 * a.force);
+    const float om = a.omega_f, om1 = a.om1_f;
+    const float c = a.c_f;
     const float uv15 = 1.5f * (u * u + v * v + w * w);
     const float base = om * delta;
     const float am = -c * (1.0f + u), a0 = -c * u, ap = c * (1.0f - u);
@@ -288,13 +290,45 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float
 
 /* --------------------------------------------------------------- kernel */
 
+/* ----------------------------------------- FP64 on the integer pipes */
+
+template <bool MACRO>
+__device__ __forceinline__ Macro collide_fx(double (&f)[Q], const StepArgs &a,
+                                            bool &fallback)
+{
+    uint64_t b[Q];
+#pragma unroll
+    for (int j = 0; j < Q; j++) b[j] = (uint64_t)__double_as_longlong(f[j]);
+    fx::Moments mm;
+    const uint32_t fl = fx::collide(b, a.fxk, a.it > 0, mm);
+    Macro m;
+    fallback = (fl & fx::kBad) != 0;
+    m.bad = (fl & fx::kDensity) != 0;
+#pragma unroll
+    for (int j = 0; j < Q; j++) f[j] = __longlong_as_double((long long)b[j]);
+    if (MACRO) {
+        uint32_t ignore = 0;
+        m.rho = __longlong_as_double((long long)fx::to_bits(mm.R, ignore));
+        m.u = (double)fx::mul(mm.Jx, mm.inv) * 0x1p-60;
+        m.v = (double)fx::mul(mm.Jy, mm.inv) * 0x1p-60;
+        m.w = (double)fx::mul(mm.Jz, mm.inv) * 0x1p-60;
+    } else {
+        m.rho = m.u = m.v = m.w = 0.0;
+    }
+    return m;
+}
+
 template <int PREC> struct StoreOf { using T = double; };
 template <> struct StoreOf<PLB_FP32> { using T = float; };
 template <> struct StoreOf<PLB_FP16DEV> { using T = __half; };
 template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
 
+/* resident blocks of 256 threads per SM the register budget is set for */
+template <int PREC> struct MinBlocks { static constexpr int v = 1; };
+template <> struct MinBlocks<PLB_FP64> { static constexpr int v = 2; };
+
 template <int PREC, bool MACRO>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, MinBlocks<PREC>::v)
 k_step(const StepArgs a)
 {
     using T = typename StoreOf<PREC>::T;
@@ -306,7 +340,19 @@ k_step(const StepArgs a)
         Macro m;
         T *fout = (T *)a.fout;
         const long long np = a.npad;
-        if constexpr (PREC == PLB_FP64_EXACT || PREC == PLB_FP64) {
+        if constexpr (PREC == PLB_FP64) {
+            bool fallback;
+            m = collide_fx<MACRO>(raw, a, fallback);
+            if (fallback) {
+                /* outside the fixed-point range: native FP64 from the
+                 * streamed values, gathered again */
+                gather<double>(a, i, raw);
+                m = collide_fp64_fma(raw, a);
+                atomicOr(a.flags, 2u);
+            }
+#pragma unroll
+            for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
+        } else if constexpr (PREC == PLB_FP64_EXACT || PREC == PLB_FP64_FMA) {
             if constexpr (PREC == PLB_FP64_EXACT) m = collide_fp64_exact(raw, a);
             else m = collide_fp64_fma(raw, a);
 #pragma unroll
@@ -375,6 +421,7 @@ cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
     switch (precision) {
     case PLB_FP64_EXACT: return launch_prec<PLB_FP64_EXACT>(macros, a, block, s);
     case PLB_FP64: return launch_prec<PLB_FP64>(macros, a, block, s);
+    case PLB_FP64_FMA: return launch_prec<PLB_FP64_FMA>(macros, a, block, s);
     case PLB_FP32: return launch_prec<PLB_FP32>(macros, a, block, s);
     case PLB_FP16DEV: return launch_prec<PLB_FP16DEV>(macros, a, block, s);
     case PLB_BF16DEV: return launch_prec<PLB_BF16DEV>(macros, a, block, s);

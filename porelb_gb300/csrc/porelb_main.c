@@ -35,6 +35,7 @@ static int parse_precision(const char *s)
     if (!strcmp(s, "fp32")) return PLB_FP32;
     if (!strcmp(s, "fp16dev")) return PLB_FP16DEV;
     if (!strcmp(s, "bf16dev")) return PLB_BF16DEV;
+    if (!strcmp(s, "fp64_fma")) return PLB_FP64_FMA;
     return -1;
 }
 

@@ -123,19 +123,37 @@ def test_chunked_steps_equal_one_call():
         assert (a.macros() == b.macros()).all()
 
 
-def test_fp64_fma_within_1e12_of_reference_c1():
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fma"])
+def test_fp64_forms_within_1e12_of_reference_c1(precision):
+    """f within 1e-12 relative and k within 1e-10 relative of the reference
+    after 1000 steps of the 64^3 plain configuration."""
     m = META["c1_64_seed0"]
     flag = pack_flag(m["dims"], 0, 6.0, 6.0, 0.40)
     V, vs = P.build_table(flag, *m["dims"], 1)
     ref = gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"])
-    fma = gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"],
-                  precision="fp64")
+    fast = gpu_run(V, m["dims"], vs, m["tau"], m["force"], m["steps"],
+                   precision=precision)
     assert sha(ref.get_f()) == m["sha_f0"]
-    assert max_rel(fma.get_f(), ref.get_f()) <= 1e-12
-    kd = fma.permeability()[0]
+    assert max_rel(fast.get_f(), ref.get_f()) <= 1e-12
+    kd = fast.permeability()[0]
     assert abs(kd - m["k_darcy"]) <= 1e-10 * abs(m["k_darcy"])
+    assert max_rel(fast.macros()[0], ref.macros()[0]) <= 1e-12
     ref.close()
-    fma.close()
+    fast.close()
+
+
+@pytest.mark.parametrize("case", [((32, 32, 32), 5, 4.0, 4.0, 0.4, 0.8, 1e-3, 300),
+                                  ((24, 20, 16), 6, 2.0, 5.0, 0.3, 0.6, 1e-4, 200)])
+def test_fp64_fixed_point_within_1e12_high_velocity(case):
+    dims, seed, rmin, rmax, phi, tau, force, steps = case
+    flag = pack_flag(dims, seed, rmin, rmax, phi)
+    V, vs = P.build_table(flag, *dims, 1)
+    s = O.OracleSim(V, *dims, vs, tau, force)
+    s.init()
+    assert s.run(steps)[0] == 0
+    with gpu_run(V, dims, vs, tau, force, steps, precision="fp64") as sim:
+        assert max_rel(sim.get_f(), s.f0()) <= 1e-12
+        assert max_rel(sim.macros()[0], s.macros()[0]) <= 1e-12
 
 
 def test_set_get_roundtrip_and_restart():
@@ -200,3 +218,35 @@ def test_empty_domain():
     with gpu_run(V, (2, 2, 2), vs, 0.8, 1e-3, 3) as sim:
         assert sim.get_f().size == 0
         assert sim.reduce() == (0.0, 0.0)
+
+
+def test_fp64_fixed_point_matches_cpu_twin_bitwise(tmp_path):
+    """The GPU's integer collision and its CPU build give identical bits."""
+    import ctypes
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = tmp_path / "fx_twin.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC",
+                    "-shared", "-o", str(so),
+                    os.path.join(here, "native", "fx_twin.cpp")], check=True)
+    lib = ctypes.CDLL(str(so))
+    v = ctypes.c_void_p
+    lib.fx_twin_step.restype = ctypes.c_int
+    lib.fx_twin_step.argtypes = [v, v, ctypes.c_int, v, v, v, v,
+                                 ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    dims = (20, 18, 16)
+    flag = pack_flag(dims, 9, 3.0, 4.0, 0.4)
+    V, vs = P.build_table(flag, *dims, 1)
+    kind, src = O.pull_table(V, vs)
+    N = len(V)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    f0 = np.tile(w, N)
+    f1, fo, mac = f0.copy(), f0.copy(), np.zeros((4, N))
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)  # noqa: E731
+    for it in range(60):
+        assert lib.fx_twin_step(p(kind), p(src), N, p(f0), p(f1), p(fo),
+                                p(mac), 0.7, 2e-4, it) == 0
+        f0, fo = fo, f0
+    with gpu_run(V, dims, vs, 0.7, 2e-4, 60, precision="fp64") as sim:
+        assert (sim.get_f() == f0).all()
+        assert (sim.macros()[0] == mac[0]).all()
