@@ -150,6 +150,26 @@ int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
                plb_sim **out);
 void plb_destroy(plb_sim *sim);
 
+/* build_V + plb_create in one device pass, from a flag grid (host buffer,
+ * values 0/1, x fastest; num_p z slabs as preprocess.c:152).  No V.bin
+ * records are formed: fluid cells are ranked in lexicographic order (the
+ * reference node numbers) and along the Morton curve on the device.  The
+ * handle is identical to plb_create on plb_build_table's output. */
+int plb_create_from_flag(const uint8_t *flag, int nx, int ny, int nz,
+                         int num_p, const plb_params *p, plb_sim **out);
+
+/* plb_sphere_pack on the device: the same flag bit for bit (flag may be
+ * NULL to only report the sphere count and porosity). */
+int plb_sphere_pack_device(uint64_t seed, int nx, int ny, int nz, double rmin,
+                           double rmax, double porosity, int device,
+                           uint8_t *flag, int *num_spheres, double *porosity_out);
+
+/* Sphere pack + table build + handle, all on the device. */
+int plb_create_packed(uint64_t seed, int nx, int ny, int nz, double rmin,
+                      double rmax, double porosity, int num_p,
+                      const plb_params *p, plb_sim **out, int *num_spheres,
+                      double *porosity_out);
+
 /* init_dist_macro (porelb.c:224-238): rho=1, u=0, f0=f1=feq. */
 int plb_init_equilibrium(plb_sim *sim);
 

@@ -2,4 +2,5 @@
 path) behind a C ABI (include/porelb_gpu.h)."""
 from ._lib import NODE_DTYPE, NB_DTYPE, Q, LIB_PATH  # noqa: F401
 from .api import (PorelbError, Simulation, build_table, check_table,  # noqa: F401
-                  read_vbin, sphere_pack, write_vbin)
+                  read_vbin, sphere_pack, sphere_pack_device,
+                  write_vbin)

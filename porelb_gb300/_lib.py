@@ -57,6 +57,13 @@ _SIGS = {
     "plb_create": (_I, [_P, _I, _I, _I, _I, _I, _IP, ctypes.POINTER(Params),
                         ctypes.POINTER(_P)]),
     "plb_destroy": (None, [_P]),
+    "plb_create_from_flag": (_I, [_P, _I, _I, _I, _I, ctypes.POINTER(Params),
+                                  ctypes.POINTER(_P)]),
+    "plb_sphere_pack_device": (_I, [ctypes.c_uint64, _I, _I, _I, _D, _D, _D,
+                                    _I, _P, _IP, _DP]),
+    "plb_create_packed": (_I, [ctypes.c_uint64, _I, _I, _I, _D, _D, _D, _I,
+                               ctypes.POINTER(Params), ctypes.POINTER(_P),
+                               _IP, _DP]),
     "plb_init_equilibrium": (_I, [_P]),
     "plb_step": (_I, [_P, _I, _I]),
     "plb_step_async": (_I, [_P, _I, _I]),

@@ -108,6 +108,32 @@ def sphere_pack(seed, nx, ny, nz, rmin, rmax, porosity):
     return flag, ns.value, phi.value
 
 
+def sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, device=0):
+    """sphere_pack on the GPU (bit-identical flag)."""
+    lib = _lib.load()
+    flag = np.zeros(nx * ny * nz, dtype=np.uint8)
+    ns = ctypes.c_int(0)
+    phi = ctypes.c_double(0.0)
+    _check(lib.plb_sphere_pack_device(ctypes.c_uint64(seed), nx, ny, nz, rmin,
+                                      rmax, porosity, device, _ptr(flag),
+                                      ctypes.byref(ns), ctypes.byref(phi)),
+           "sphere_pack_device")
+    return flag, ns.value, phi.value
+
+
+def _params(tau, force, precision, ordering, halo, block_size, device):
+    lib = _lib.load()
+    p = _lib.Params()
+    lib.plb_default_params(ctypes.byref(p))
+    p.tau, p.force_x = float(tau), float(force)
+    p.precision = PRECISIONS[precision]
+    p.ordering = ORDERINGS[ordering]
+    p.halo = HALOS[halo]
+    p.block_size = block_size
+    p.device = device
+    return p
+
+
 # ------------------------------------------------------------------ solver
 
 class Simulation:
@@ -216,6 +242,52 @@ class Simulation:
                                   ctypes.byref(prec), ctypes.byref(b)), "info")
         return dict(num_node=n.value, npad=npad.value, precision=prec.value,
                     device_bytes=b.value)
+
+    @classmethod
+    def _from_handle(cls, h, nx, ny, nz, tau, force, precision):
+        self = cls.__new__(cls)
+        self._lib = _lib.load()
+        self._h = h
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.tau, self.force, self.precision = float(tau), float(force), precision
+        self.N = self.info()["num_node"]
+        self.V = None
+        self.it = 0
+        return self
+
+    @classmethod
+    def from_flag(cls, flag, nx, ny, nz, num_p=1, tau=0.8, force=1e-3,
+                  precision="fp64_exact", ordering="morton", halo="auto",
+                  block_size=0, device=0):
+        """build_V + create on the device from a 0/1 flag grid."""
+        lib = _lib.load()
+        flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
+        if flag.size != nx * ny * nz:
+            raise ValueError("flag size does not match nx*ny*nz")
+        p = _params(tau, force, precision, ordering, halo, block_size, device)
+        h = ctypes.c_void_p()
+        _check(lib.plb_create_from_flag(_ptr(flag), nx, ny, nz, num_p,
+                                        ctypes.byref(p), ctypes.byref(h)),
+               "plb_create_from_flag")
+        return cls._from_handle(h, nx, ny, nz, tau, force, precision)
+
+    @classmethod
+    def packed(cls, seed, nx, ny, nz, rmin, rmax, porosity, num_p=1, tau=0.8,
+               force=1e-3, precision="fp64", ordering="morton", halo="auto",
+               block_size=0, device=0):
+        """Sphere pack, table and handle, all built on the device."""
+        lib = _lib.load()
+        p = _params(tau, force, precision, ordering, halo, block_size, device)
+        h = ctypes.c_void_p()
+        ns = ctypes.c_int(0)
+        phi = ctypes.c_double(0.0)
+        _check(lib.plb_create_packed(ctypes.c_uint64(seed), nx, ny, nz, rmin,
+                                     rmax, porosity, num_p, ctypes.byref(p),
+                                     ctypes.byref(h), ctypes.byref(ns),
+                                     ctypes.byref(phi)), "plb_create_packed")
+        sim = cls._from_handle(h, nx, ny, nz, tau, force, precision)
+        sim.num_spheres, sim.porosity = ns.value, phi.value
+        return sim
 
     @property
     def stream(self):

@@ -144,6 +144,32 @@ FX_HD uint64_t to_bits(int64_t F, uint32_t &rmax_seen)
     return ((uint64_t)(ef + 867u) << 52) + q;
 }
 
+/* Fast forms for a value whose FP64 exponent is E (biased) in the common
+ * case: the shift is a constant.  Each reports, through *off, whether the
+ * value left that binade (then the general form above is used). */
+template <uint32_t E>
+FX_HD int64_t from_bits_e(uint64_t b, uint32_t &smax_seen)
+{
+    const uint32_t hi = (uint32_t)(b >> 32);
+    if ((hi >> 20) == E) {
+        const uint64_t m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+        return (int64_t)(m << (E - 1015u));
+    }
+    return from_bits(b, smax_seen);
+}
+
+/* to_bits for a result expected in the binade of exponent E */
+template <uint32_t E>
+FX_HD uint64_t to_bits_e(int64_t F, uint32_t &rmax_seen)
+{
+    /* F in [2^(E-963), 2^(E-962)) has E-962 bits: drop E-1015 of them */
+    const uint64_t u = (uint64_t)F;
+    const uint64_t q = (u + (((uint64_t)1 << (E - 1015u)) >> 1)) >> (E - 1015u);
+    if ((q >> 52) == 1u) /* q in [2^52, 2^53): still in the binade */
+        return ((uint64_t)(E - 1u) << 52) + q;
+    return to_bits(F, rmax_seen);
+}
+
 /* Q60 of a positive normal float in [2^-8, 4) */
 FX_HD int64_t from_float(float x)
 {
@@ -225,9 +251,11 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
 {
     uint32_t s0 = 0, s12 = 0, rmax = 0;
     int64_t F[19];
-    F[0] = from_bits(bits[0], s0);
+    /* the binades of the weights: 1/3 -> 1021, 1/18 -> 1018, 1/36 -> 1017 */
+    F[0] = from_bits_e<1021>(bits[0], s0);
 #pragma unroll
-    for (int j = 1; j < 19; j++) F[j] = from_bits(bits[j], s12);
+    for (int j = 1; j < 19; j++)
+        F[j] = j <= 6 ? from_bits_e<1018>(bits[j], s12) : from_bits_e<1017>(bits[j], s12);
 
     /* exact moments: rho and J from pair sums / differences */
     int64_t R = F[0], Jx = 0, Jy = 0, Jz = 0;
@@ -283,7 +311,7 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t qd = -mul(split(JJ15), INVs);
         const int64_t G = W00 + mul(T00, split(qd));
         const int64_t Fn = F[0] - mul(oms, split(F[0] - k.tp[0])) + G;
-        bits[0] = to_bits(Fn, rmax);
+        bits[0] = to_bits_e<1021>(Fn, rmax);
     }
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
@@ -312,8 +340,13 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t GK = WK + mul(TK, split(qd - t3));
         const int64_t FnJ = F[J] - mul(oms, split(F[J] - tpc)) + GJ;
         const int64_t FnK = F[K] - mul(oms, split(F[K] - tpc)) + GK;
-        bits[J] = to_bits(FnJ, rmax);
-        bits[K] = to_bits(FnK, rmax);
+        if (c == 1) {
+            bits[J] = to_bits_e<1018>(FnJ, rmax);
+            bits[K] = to_bits_e<1018>(FnK, rmax);
+        } else {
+            bits[J] = to_bits_e<1017>(FnJ, rmax);
+            bits[K] = to_bits_e<1017>(FnK, rmax);
+        }
     }
     const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u);
     return flags | (bad ? kBad : 0u);

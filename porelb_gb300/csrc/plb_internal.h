@@ -71,6 +71,21 @@ struct StepArgs {
     unsigned int *flags;     /* bit 0: FP16 scale overflow */
 };
 
+/* Exclusive scan of m uint32 counts into offs (device memory). */
+int scan_words(const uint32_t *cnt, uint32_t *offs, size_t m, cudaStream_t st);
+
+/* Device geometry (plb_geom.cu). */
+int sphere_pack_device(uint64_t seed, int nx, int ny, int nz, double rmin,
+                       double rmax, double porosity, uint8_t *dflag,
+                       int *num_spheres, double *porosity_out, cudaStream_t st);
+int flag_rank(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
+              uint32_t *lexbits, uint32_t *lexoffs, int *n, int *slab_start,
+              cudaStream_t st);
+int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
+                int ordering, int remote_wins, const uint32_t *lexbits,
+                const uint32_t *lexoffs, int n, long long npad, int *perm,
+                uint16_t *coord, uint32_t *nbr, cudaStream_t st);
+
 /* Launch one step of the given precision. */
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
                         int block, cudaStream_t s);

@@ -165,6 +165,19 @@ static int exclusive_scan(const uint32_t *in, uint32_t *out, size_t m,
     return PLB_OK;
 }
 
+namespace plb {
+int scan_words(const uint32_t *cnt, uint32_t *offs, size_t m, cudaStream_t st)
+{
+    const size_t ntiles = (m + kScanTile - 1) / kScanTile;
+    uint32_t *tmp = nullptr;
+    if (cudaMalloc(&tmp, ntiles * 4 + 4) != cudaSuccess) return PLB_ERR_NOMEM;
+    int rc = exclusive_scan(cnt, offs, m, tmp, st);
+    cudaStreamSynchronize(st);
+    cudaFree(tmp);
+    return rc;
+}
+}  // namespace plb
+
 /* --------------------------------------------------------- table build */
 
 struct MortonBits {
@@ -582,27 +595,21 @@ done:
     return rc;
 }
 
-int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
-               int num_p, const int *v_sub_start, const plb_params *p,
-               plb_sim **out)
+/* Validate the parameters, create the handle and allocate its device arrays
+ * for n nodes (everything but the tables). */
+static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
+                     int num_p, const int *v_sub_start, plb_sim **out)
 {
-    if (!out) return PLB_ERR_ARG;
     *out = nullptr;
-    plb_params defp;
-    if (!p) {
-        plb_default_params(&defp);
-        p = &defp;
-    }
-    if (num_node < 0 || (num_node > 0 && !V) || nx <= 0 || ny <= 0 || nz <= 0 ||
-        num_p <= 0 || !v_sub_start || !(p->tau > 0.5) || !isfinite(p->force_x) ||
-        elem_size(p->precision) == 0 ||
+    if (n < 0 || nx <= 0 || ny <= 0 || nz <= 0 || num_p <= 0 || !v_sub_start ||
+        !(p->tau > 0.5) || !isfinite(p->force_x) || elem_size(p->precision) == 0 ||
         (p->ordering != PLB_ORDER_MORTON && p->ordering != PLB_ORDER_REFERENCE) ||
-        num_node >= (int)kSrcMask)
+        n >= (int)kSrcMask)
         return PLB_ERR_ARG;
     if (v_sub_start[0] != 0) return PLB_ERR_NUMP;
     for (int q = 0; q < num_p; q++) {
-        const int hi = q + 1 < num_p ? v_sub_start[q + 1] : num_node;
-        if (v_sub_start[q] < 0 || hi < v_sub_start[q] || hi > num_node) return PLB_ERR_NUMP;
+        const int hi = q + 1 < num_p ? v_sub_start[q + 1] : n;
+        if (v_sub_start[q] < 0 || hi < v_sub_start[q] || hi > n) return PLB_ERR_NUMP;
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || p->device < 0 ||
@@ -613,10 +620,10 @@ int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
     CK(cudaSetDevice(p->device));
     plb_sim *s = (plb_sim *)calloc(1, sizeof(plb_sim));
     if (!s) return PLB_ERR_NOMEM;
-    s->n = num_node;
+    s->n = n;
     s->nx = nx; s->ny = ny; s->nz = nz;
     s->num_p = num_p;
-    s->npad = ((long long)num_node + 1 + 63) / 64 * 64;
+    s->npad = ((long long)n + 1 + 63) / 64 * 64;
     s->precision = p->precision;
     s->ordering = p->ordering;
     s->halo = p->halo;
@@ -633,10 +640,9 @@ int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
     s->v_sub_start = (int *)malloc(sizeof(int) * (size_t)(num_p + 1));
     if (!s->v_sub_start) { free(s); return PLB_ERR_NOMEM; }
     memcpy(s->v_sub_start, v_sub_start, sizeof(int) * (size_t)num_p);
-    s->v_sub_start[num_p] = num_node;
-    s->nblocks = (int)nblk(num_node > 0 ? num_node : 1, s->block);
+    s->v_sub_start[num_p] = n;
+    s->nblocks = (int)nblk(n > 0 ? n : 1, s->block);
 
-    int rc = PLB_OK;
     size_t acc = 0;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     const size_t fbytes = s->elem * Q * (size_t)s->npad;
@@ -656,19 +662,168 @@ int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
         return e == cudaErrorMemoryAllocation ? PLB_ERR_NOMEM : PLB_ERR_CUDA;
     }
     s->dev_bytes = acc;
-    rc = build_tables(s, V);
+    *out = s;
+    return PLB_OK;
+}
+
+static int sim_finish(plb_sim *s, int rc, plb_sim **out)
+{
     if (rc == PLB_OK) {
-        e = cudaMemsetAsync(s->err, 0xff, 8, s->stream);
+        cudaError_t e = cudaMemsetAsync(s->err, 0xff, 8, s->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->flags, 0, 4, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) rc = PLB_ERR_CUDA;
     }
     if (rc != PLB_OK) {
         free_sim(s);
+        *out = nullptr;
         return rc;
     }
     *out = s;
     return PLB_OK;
+}
+
+int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
+               int num_p, const int *v_sub_start, const plb_params *p,
+               plb_sim **out)
+{
+    if (!out) return PLB_ERR_ARG;
+    *out = nullptr;
+    plb_params defp;
+    if (!p) {
+        plb_default_params(&defp);
+        p = &defp;
+    }
+    if (num_node < 0 || (num_node > 0 && !V)) return PLB_ERR_ARG;
+    plb_sim *s = nullptr;
+    int rc = sim_alloc(p, num_node, nx, ny, nz, num_p, v_sub_start, &s);
+    if (rc != PLB_OK) return rc;
+    return sim_finish(s, build_tables(s, V), out);
+}
+
+/* Tables from a flag grid already on the device. */
+static int create_from_dflag(const uint8_t *dflag, int nx, int ny, int nz,
+                             int num_p, const plb_params *p, cudaStream_t st,
+                             plb_sim **out)
+{
+    const size_t cells = (size_t)nx * ny * nz;
+    const size_t words = (cells + 31) / 32;
+    uint32_t *lexbits = nullptr, *lexoffs = nullptr;
+    int *slab = (int *)calloc((size_t)num_p + 1, sizeof(int));
+    int rc = PLB_OK, n = 0;
+    plb_sim *s = nullptr;
+    if (!slab) return PLB_ERR_NOMEM;
+    if (cudaMalloc(&lexbits, words * 4) != cudaSuccess ||
+        cudaMalloc(&lexoffs, words * 4) != cudaSuccess) {
+        rc = PLB_ERR_NOMEM;
+    }
+    if (rc == PLB_OK)
+        rc = flag_rank(dflag, nx, ny, nz, num_p, lexbits, lexoffs, &n, slab, st);
+    if (rc == PLB_OK) rc = sim_alloc(p, n, nx, ny, nz, num_p, slab, &s);
+    if (rc == PLB_OK) {
+        const int remote_wins = (s->halo == PLB_HALO_REMOTE_WINS) ||
+                                (s->halo == PLB_HALO_AUTO && s->num_p > 1);
+        rc = flag_tables(dflag, nx, ny, nz, num_p, s->ordering, remote_wins, lexbits,
+                         lexoffs, n, s->npad, s->perm, s->coord, s->nbr, st);
+        rc = sim_finish(s, rc, out);
+    }
+    cudaFree(lexbits);
+    cudaFree(lexoffs);
+    free(slab);
+    return rc;
+}
+
+int plb_create_from_flag(const uint8_t *flag, int nx, int ny, int nz,
+                         int num_p, const plb_params *p, plb_sim **out)
+{
+    if (!out) return PLB_ERR_ARG;
+    *out = nullptr;
+    plb_params defp;
+    if (!p) {
+        plb_default_params(&defp);
+        p = &defp;
+    }
+    if (!flag || nx <= 0 || ny <= 0 || nz <= 0 || nx > 65536 || ny > 65536 ||
+        nz > 65536 || num_p <= 0 || num_p > nz || nz % num_p)
+        return PLB_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || p->device < 0 ||
+        p->device >= ndev)
+        return PLB_ERR_CUDA;
+    CK(cudaSetDevice(p->device));
+    const size_t cells = (size_t)nx * ny * nz;
+    uint8_t *dflag = nullptr;
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int rc = PLB_OK;
+    if (cudaMalloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
+    if (rc == PLB_OK && cudaMemcpyAsync(dflag, flag, cells, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        rc = PLB_ERR_CUDA;
+    if (rc == PLB_OK) rc = create_from_dflag(dflag, nx, ny, nz, num_p, p, st, out);
+    cudaStreamSynchronize(st);
+    cudaFree(dflag);
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+int plb_sphere_pack_device(uint64_t seed, int nx, int ny, int nz, double rmin,
+                           double rmax, double porosity, int device,
+                           uint8_t *flag, int *num_spheres, double *porosity_out)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0 || !(rmin > 0.0) || rmax < rmin ||
+        !(porosity >= 0.0) || !(porosity <= 1.0))
+        return PLB_ERR_ARG;
+    CK(cudaSetDevice(device));
+    const size_t cells = (size_t)nx * ny * nz;
+    uint8_t *dflag = nullptr;
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int rc = PLB_OK;
+    if (cudaMalloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
+    if (rc == PLB_OK)
+        rc = sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, dflag,
+                                num_spheres, porosity_out, st);
+    if (rc == PLB_OK && flag &&
+        (cudaMemcpyAsync(flag, dflag, cells, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+         cudaStreamSynchronize(st) != cudaSuccess))
+        rc = PLB_ERR_CUDA;
+    cudaStreamSynchronize(st);
+    cudaFree(dflag);
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+int plb_create_packed(uint64_t seed, int nx, int ny, int nz, double rmin,
+                      double rmax, double porosity, int num_p,
+                      const plb_params *p, plb_sim **out, int *num_spheres,
+                      double *porosity_out)
+{
+    if (!out) return PLB_ERR_ARG;
+    *out = nullptr;
+    plb_params defp;
+    if (!p) {
+        plb_default_params(&defp);
+        p = &defp;
+    }
+    if (nx <= 0 || ny <= 0 || nz <= 0 || nx > 65536 || ny > 65536 || nz > 65536 ||
+        num_p <= 0 || num_p > nz || nz % num_p || !(rmin > 0.0) || rmax < rmin ||
+        !(porosity >= 0.0) || !(porosity <= 1.0))
+        return PLB_ERR_ARG;
+    CK(cudaSetDevice(p->device));
+    const size_t cells = (size_t)nx * ny * nz;
+    uint8_t *dflag = nullptr;
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int rc = PLB_OK;
+    if (cudaMalloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
+    if (rc == PLB_OK)
+        rc = sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, dflag,
+                                num_spheres, porosity_out, st);
+    if (rc == PLB_OK) rc = create_from_dflag(dflag, nx, ny, nz, num_p, p, st, out);
+    cudaStreamSynchronize(st);
+    cudaFree(dflag);
+    cudaStreamDestroy(st);
+    return rc;
 }
 
 int plb_init_equilibrium(plb_sim *s)
