@@ -215,6 +215,56 @@ int plb_info(plb_sim *sim, int *num_node, int *npad, int *precision,
              size_t *device_bytes);
 void *plb_stream(plb_sim *sim);
 
+/* ---------------------------------------------------------------- batch */
+
+/* Many independent samples in one device node pool (no reference
+ * counterpart; each sample runs porelb's step loop).  Samples are admitted
+ * into free 256-node block ranges, stepped together K steps at a time (one
+ * CUDA graph per interval), checked for steady state after each interval
+ * (|<u_x>(t) - <u_x>(t-K)| <= tol |<u_x>(t)|) and retired. */
+typedef struct plb_batch plb_batch;
+
+typedef struct {
+    double tau;          /* relaxation time of the sample */
+    double force_x;      /* body force of the sample */
+    double tol;          /* steady-state tolerance on <u_x> over one interval */
+    long long max_steps; /* stop after this many steps (<= 0: no limit) */
+    int reserved[4];
+} plb_sample_params;
+
+/* Device bytes per pool node for a storage form (the admission unit). */
+size_t plb_batch_bytes_per_node(int precision, int keep_macros);
+/* capacity_nodes: pool size; check_every: interval K (even); keep_macros: also
+ * keep rho/u per node for plb_batch_get_macros. */
+int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
+                     int check_every, int keep_macros, int device,
+                     plb_batch **out);
+void plb_batch_destroy(plb_batch *b);
+/* Admit a sample from a host flag grid (0/1) or a device sphere pack.
+ * PLB_ERR_NOMEM when no free range or sample slot is left. */
+int plb_batch_add_flag(plb_batch *b, const uint8_t *flag, int nx, int ny,
+                       int nz, const plb_sample_params *sp, int *id);
+int plb_batch_add_packed(plb_batch *b, uint64_t seed, int nx, int ny, int nz,
+                         double rmin, double rmax, double porosity,
+                         const plb_sample_params *sp, int *id,
+                         int *num_spheres, double *porosity_out);
+/* Run `intervals` intervals of K steps (stops early when nothing is active). */
+int plb_batch_run(plb_batch *b, int intervals, int *n_active);
+/* Ids of samples that finished since the last poll. */
+int plb_batch_poll(plb_batch *b, int *ids, int max_ids, int *count);
+/* status: 0 running, 1 converged, 2 step limit, 3 released, <0 error. */
+int plb_batch_result(plb_batch *b, int id, double *k_darcy, double *mean_ux,
+                     long long *steps, int *status);
+int plb_batch_release(plb_batch *b, int id);
+int plb_batch_get_f(plb_batch *b, int id, double *f_aos);
+int plb_batch_get_macros(plb_batch *b, int id, double *rho, double *ux,
+                         double *uy, double *uz);
+int plb_batch_info(plb_batch *b, long long *t, int *active,
+                   long long *used_nodes, long long *capacity_nodes,
+                   size_t *device_bytes);
+int plb_batch_sample_nodes(plb_batch *b, int id, int *num_node);
+void *plb_batch_stream(plb_batch *b);
+
 /* Human-readable text for a status code. */
 const char *plb_status_string(int status);
 

@@ -39,6 +39,12 @@ class Params(ctypes.Structure):
                 ("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
+class SampleParams(ctypes.Structure):
+    _fields_ = [("tau", ctypes.c_double), ("force_x", ctypes.c_double),
+                ("tol", ctypes.c_double), ("max_steps", ctypes.c_longlong),
+                ("reserved", ctypes.c_int * 4)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -78,6 +84,28 @@ _SIGS = {
     "plb_info": (_I, [_P, _IP, _IP, _IP, ctypes.POINTER(ctypes.c_size_t)]),
     "plb_stream": (_P, [_P]),
     "plb_status_string": (ctypes.c_char_p, [_I]),
+    "plb_batch_bytes_per_node": (ctypes.c_size_t, [_I, _I]),
+    "plb_batch_create": (_I, [ctypes.c_size_t, _I, _I, _I, _I, _I,
+                              ctypes.POINTER(_P)]),
+    "plb_batch_destroy": (None, [_P]),
+    "plb_batch_add_flag": (_I, [_P, _P, _I, _I, _I,
+                                ctypes.POINTER(SampleParams), _IP]),
+    "plb_batch_add_packed": (_I, [_P, ctypes.c_uint64, _I, _I, _I, _D, _D, _D,
+                                  ctypes.POINTER(SampleParams), _IP, _IP,
+                                  _DP]),
+    "plb_batch_run": (_I, [_P, _I, _IP]),
+    "plb_batch_poll": (_I, [_P, _IP, _I, _IP]),
+    "plb_batch_result": (_I, [_P, _I, _DP, _DP,
+                              ctypes.POINTER(ctypes.c_longlong), _IP]),
+    "plb_batch_release": (_I, [_P, _I]),
+    "plb_batch_get_f": (_I, [_P, _I, _P]),
+    "plb_batch_get_macros": (_I, [_P, _I, _P, _P, _P, _P]),
+    "plb_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), _IP,
+                            ctypes.POINTER(ctypes.c_longlong),
+                            ctypes.POINTER(ctypes.c_longlong),
+                            ctypes.POINTER(ctypes.c_size_t)]),
+    "plb_batch_sample_nodes": (_I, [_P, _I, _IP]),
+    "plb_batch_stream": (_P, [_P]),
 }
 
 _lib = None

@@ -7,7 +7,7 @@
  * Q60 fixed point (int64 holding value * 2^60): the distributions are
  * converted exactly from their FP64 bits, the moments are exact integer
  * sums, products are 64x64 -> (128 >> 60) built from three 32-bit wide
- * multiplies (error <= 2.5 * 2^-60 each, zero mean), and the results are
+ * multiply-adds (error <= 1 * 2^-60 each, zero mean), and the results are
  * rounded back to FP64.  Against the reference's FP64 arithmetic the
  * per-step difference is a fraction of an FP64 ulp of the weights, the same
  * order as the reference's own rounding.
@@ -48,7 +48,7 @@ namespace fx {
 
 constexpr int64_t kOne = (int64_t)1 << 60;
 
-/* a = h * 2^31 + l with 0 <= l < 2^31 */
+/* a = h * 2^30 + l with 0 <= l < 2^30 (|h| < 2^31 for |a| < 2^61) */
 struct Sp {
     int32_t h;
     int32_t l;
@@ -57,23 +57,23 @@ struct Sp {
 FX_HD Sp split(int64_t a)
 {
     Sp s;
-    s.h = (int32_t)(a >> 31);
-    s.l = (int32_t)((uint32_t)a & 0x7fffffffu);
+    s.h = (int32_t)(a >> 30);
+    s.l = (int32_t)((uint32_t)a & 0x3fffffffu);
     return s;
 }
 
 FX_HD int64_t wmul(int32_t a, int32_t b) { return (int64_t)a * (int64_t)b; }
 
 /* a * b / 2^60 for |a|, |b| < 2^61 (values of magnitude < 2), from three
- * 32x32 -> 64 multiplies:
- *   a*b = ah bh 2^62 + (ah bl + al bh) 2^31 + al bl.
- * The al bl term (in [0, 2^62)) is replaced by its mean 2^60 and the sum is
+ * 32x32 -> 64 multiply-adds:
+ *   a*b / 2^60 = ah bh + (ah bl + al bh) / 2^30 + al bl / 2^60.
+ * The last term (in [0, 1)) is replaced by its mean 1/4 and the middle one
  * rounded to nearest, which is the constant 3*2^28 added before the shift:
- * |error| <= 2.5 units of 2^-60, zero on average. */
+ * |error| <= 1 unit of 2^-60, zero on average. */
 FX_HD int64_t mul(Sp a, Sp b)
 {
     const int64_t mid = wmul(a.h, b.l) + wmul(a.l, b.h) + ((int64_t)3 << 28);
-    return wmul(a.h, b.h) * 4 + (mid >> 29);
+    return wmul(a.h, b.h) + (mid >> 30);
 }
 
 FX_HD int64_t mul(int64_t a, int64_t b) { return mul(split(a), split(b)); }
@@ -142,32 +142,6 @@ FX_HD uint64_t to_bits(int64_t F, uint32_t &rmax_seen)
     const uint32_t rr = r & 15u;
     const uint64_t q = (u + ((1u << rr) >> 1)) >> rr; /* [2^52, 2^53] */
     return ((uint64_t)(ef + 867u) << 52) + q;
-}
-
-/* Fast forms for a value whose FP64 exponent is E (biased) in the common
- * case: the shift is a constant.  Each reports, through *off, whether the
- * value left that binade (then the general form above is used). */
-template <uint32_t E>
-FX_HD int64_t from_bits_e(uint64_t b, uint32_t &smax_seen)
-{
-    const uint32_t hi = (uint32_t)(b >> 32);
-    if ((hi >> 20) == E) {
-        const uint64_t m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
-        return (int64_t)(m << (E - 1015u));
-    }
-    return from_bits(b, smax_seen);
-}
-
-/* to_bits for a result expected in the binade of exponent E */
-template <uint32_t E>
-FX_HD uint64_t to_bits_e(int64_t F, uint32_t &rmax_seen)
-{
-    /* F in [2^(E-963), 2^(E-962)) has E-962 bits: drop E-1015 of them */
-    const uint64_t u = (uint64_t)F;
-    const uint64_t q = (u + (((uint64_t)1 << (E - 1015u)) >> 1)) >> (E - 1015u);
-    if ((q >> 52) == 1u) /* q in [2^52, 2^53): still in the binade */
-        return ((uint64_t)(E - 1u) << 52) + q;
-    return to_bits(F, rmax_seen);
 }
 
 /* Q60 of a positive normal float in [2^-8, 4) */
@@ -251,11 +225,9 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
 {
     uint32_t s0 = 0, s12 = 0, rmax = 0;
     int64_t F[19];
-    /* the binades of the weights: 1/3 -> 1021, 1/18 -> 1018, 1/36 -> 1017 */
-    F[0] = from_bits_e<1021>(bits[0], s0);
+    F[0] = from_bits(bits[0], s0);
 #pragma unroll
-    for (int j = 1; j < 19; j++)
-        F[j] = j <= 6 ? from_bits_e<1018>(bits[j], s12) : from_bits_e<1017>(bits[j], s12);
+    for (int j = 1; j < 19; j++) F[j] = from_bits(bits[j], s12);
 
     /* exact moments: rho and J from pair sums / differences */
     int64_t R = F[0], Jx = 0, Jy = 0, Jz = 0;
@@ -311,7 +283,7 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t qd = -mul(split(JJ15), INVs);
         const int64_t G = W00 + mul(T00, split(qd));
         const int64_t Fn = F[0] - mul(oms, split(F[0] - k.tp[0])) + G;
-        bits[0] = to_bits_e<1021>(Fn, rmax);
+        bits[0] = to_bits(Fn, rmax);
     }
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
@@ -340,13 +312,8 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t GK = WK + mul(TK, split(qd - t3));
         const int64_t FnJ = F[J] - mul(oms, split(F[J] - tpc)) + GJ;
         const int64_t FnK = F[K] - mul(oms, split(F[K] - tpc)) + GK;
-        if (c == 1) {
-            bits[J] = to_bits_e<1018>(FnJ, rmax);
-            bits[K] = to_bits_e<1018>(FnK, rmax);
-        } else {
-            bits[J] = to_bits_e<1017>(FnJ, rmax);
-            bits[K] = to_bits_e<1017>(FnK, rmax);
-        }
+        bits[J] = to_bits(FnJ, rmax);
+        bits[K] = to_bits(FnK, rmax);
     }
     const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u);
     return flags | (bad ? kBad : 0u);

@@ -118,6 +118,7 @@ __global__ void k_assign_from_flag(const uint32_t *lexbits, const uint32_t *lexo
 __global__ void k_nbr_from_flag(const uint32_t *lexbits, const uint32_t *obits,
                                 const uint32_t *ooffs, Grid g, int slab,
                                 int remote_wins, int n, long long npad,
+                                uint32_t word_base, uint32_t rest_word,
                                 const uint16_t *coord, uint32_t *nbr)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -141,11 +142,11 @@ __global__ void k_nbr_from_flag(const uint32_t *lexbits, const uint32_t *obits,
         const bool remote = remote_wins && (sz / slab != z / slab);
         uint32_t word;
         if (push && (!bounce || remote || cs > cx))
-            word = rank_in(obits, ooffs, device_key(g, sx, sy, sz));
+            word = word_base + rank_in(obits, ooffs, device_key(g, sx, sy, sz));
         else if (bounce)
             word = kBounce;
         else
-            word = (uint32_t)n;
+            word = rest_word;
         nbr[(long long)(j - 1) * npad + k] = word;
     }
 }
@@ -384,7 +385,8 @@ done:
 int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
                 int ordering, int remote_wins, const uint32_t *lexbits,
                 const uint32_t *lexoffs, int n, long long npad, int *perm,
-                uint16_t *coord, uint32_t *nbr, cudaStream_t st)
+                uint16_t *coord, uint32_t *nbr, uint32_t word_base,
+                uint32_t rest_word, cudaStream_t st)
 {
     (void)dflag;
     const size_t cells = (size_t)nx * ny * nz;
@@ -411,7 +413,8 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
                                                        cells, n, npad, perm, coord);
     CKG(cudaGetLastError());
     k_nbr_from_flag<<<gsz((size_t)n, 128), 128, 0, st>>>(lexbits, obits, ooffs, g, nz / num_p,
-                                                        remote_wins, n, npad, coord, nbr);
+                                                        remote_wins, n, npad, word_base,
+                                                        rest_word, coord, nbr);
     CKG(cudaGetLastError());
     CKG(cudaStreamSynchronize(st));
 done:

@@ -354,5 +354,5 @@ void plb_host_constants(double tau, double force, double *omega, double *om1,
     *om1 = 1.0 - w;                    /* (1.0-omega), porelb.c:361 */
     *k3 = (1.0 - 0.5 * w) * 3.0;       /* (1.0-0.5*omega)*3.0, porelb.c:362 */
     *half_force = 0.5 * force;         /* porelb.c:348 */
-    *nu = 1.0 / 3.0 * (tau - 0.5);     /* porelb.c:89 */
+    if (nu) *nu = 1.0 / 3.0 * (tau - 0.5); /* porelb.c:89 */
 }

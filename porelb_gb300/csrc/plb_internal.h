@@ -49,6 +49,17 @@ __host__ __device__ constexpr int wclass(int j)
 constexpr uint32_t kBounce = 0x80000000u;
 constexpr uint32_t kSrcMask = 0x7fffffffu;
 
+/* Per-solve collision coefficients (host-computed from tau and F). */
+struct Coeffs {
+    /* FP64, in the reference's operation order */
+    double omega, om1, k3, force, half_force;
+    /* FP32 forms (rounded from the FP64 values) */
+    float omega_f, om1_f, c_f, half_force_f;
+    float scale, inv_scale; /* deviation storage scale */
+    fx::Consts fxk;         /* fixed-point form */
+    int it;                 /* iteration number (the it > 0 rule) */
+};
+
 struct StepArgs {
     const void *fin;
     void *fout;
@@ -56,19 +67,34 @@ struct StepArgs {
     const int *perm;      /* new -> reference index (density guard report) */
     long long npad;
     int n;
-    int it;
-    /* FP64 constants, computed on the host in the reference's order */
-    double omega, om1, k3, force, half_force;
-    /* FP32 forms (host-rounded from the FP64 constants) */
-    float scale, inv_scale;
-    float omega_f, om1_f, c_f, half_force_f;
-    /* fixed-point form */
-    fx::Consts fxk;
+    Coeffs co;
     /* macros (rho, ux, uy, uz; stride npad) and per-block sums, or NULL */
     double *macro;
     double *partial;  /* [2][gridDim.x]: sum ux, sum rho */
     unsigned long long *err; /* min over (it << 32 | reference index) */
-    unsigned int *flags;     /* bit 0: FP16 scale overflow */
+    unsigned int *flags;     /* bit 0: FP16 scale overflow, bit 1: fallback */
+};
+
+/* One sample of a batch (device copy). */
+struct SampleDev {
+    Coeffs co;
+    long long base; /* first node of the sample in the pool */
+    int n;          /* fluid nodes */
+    int start;      /* batch step at which the sample started */
+};
+
+struct BatchArgs {
+    const void *fin;
+    void *fout;
+    const uint32_t *nbr;
+    long long npad;
+    const int *blk_sample;     /* sample of every 256-node block, -1 = free */
+    const SampleDev *samples;
+    const int *t_base;         /* batch step counter (device) */
+    int t_off;                 /* this launch's step = *t_base + t_off */
+    double *macro;             /* may be NULL */
+    double *partial;           /* [3][gridDim.x]: sum ux, sum rho, max |dev| */
+    unsigned int *serr;        /* per-sample error bits */
 };
 
 /* Exclusive scan of m uint32 counts into offs (device memory). */
@@ -84,11 +110,20 @@ int flag_rank(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
 int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
                 int ordering, int remote_wins, const uint32_t *lexbits,
                 const uint32_t *lexoffs, int n, long long npad, int *perm,
-                uint16_t *coord, uint32_t *nbr, cudaStream_t st);
+                uint16_t *coord, uint32_t *nbr, uint32_t word_base,
+                uint32_t rest_word, cudaStream_t st);
 
 /* Launch one step of the given precision. */
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
                         int block, cudaStream_t s);
+
+/* One step of every active block of a batch pool (256 nodes per block). */
+constexpr int kBatchBlock = 256;
+cudaError_t launch_batch_step(int precision, bool macros, const BatchArgs &a,
+                              int nblocks, cudaStream_t s);
+
+/* Fill the coefficients from tau, F and the storage scale. */
+void make_coeffs(double tau, double force, float scale, Coeffs *c);
 
 }  // namespace plb
 

@@ -166,6 +166,21 @@ static int exclusive_scan(const uint32_t *in, uint32_t *out, size_t m,
 }
 
 namespace plb {
+void make_coeffs(double tau, double force, float scale, Coeffs *c)
+{
+    memset(c, 0, sizeof(*c));
+    plb_host_constants(tau, force, &c->omega, &c->om1, &c->k3, &c->half_force,
+                       nullptr);
+    c->force = force;
+    c->omega_f = (float)c->omega;
+    c->om1_f = (float)c->om1;
+    c->c_f = (float)(c->k3 * force);
+    c->half_force_f = (float)c->half_force;
+    c->scale = scale;
+    c->inv_scale = 1.0f / scale;
+    c->fxk = fx::make_consts(tau, force);
+}
+
 int scan_words(const uint32_t *cnt, uint32_t *offs, size_t m, cudaStream_t st)
 {
     const size_t ntiles = (m + kScanTile - 1) / kScanTile;
@@ -724,7 +739,8 @@ static int create_from_dflag(const uint8_t *dflag, int nx, int ny, int nz,
         const int remote_wins = (s->halo == PLB_HALO_REMOTE_WINS) ||
                                 (s->halo == PLB_HALO_AUTO && s->num_p > 1);
         rc = flag_tables(dflag, nx, ny, nz, num_p, s->ordering, remote_wins, lexbits,
-                         lexoffs, n, s->npad, s->perm, s->coord, s->nbr, st);
+                         lexoffs, n, s->npad, s->perm, s->coord, s->nbr, 0u,
+                         (uint32_t)n, st);
         rc = sim_finish(s, rc, out);
     }
     cudaFree(lexbits);
@@ -873,18 +889,7 @@ int plb_step_async(plb_sim *s, int it_begin, int nsteps)
     a.perm = s->perm;
     a.npad = s->npad;
     a.n = s->n;
-    a.omega = s->omega;
-    a.om1 = s->om1;
-    a.k3 = s->k3;
-    a.force = s->force;
-    a.half_force = s->half_force;
-    a.scale = s->scale;
-    a.inv_scale = 1.0f / s->scale;
-    a.omega_f = (float)s->omega;
-    a.om1_f = (float)s->om1;
-    a.c_f = (float)(s->k3 * s->force);
-    a.half_force_f = (float)s->half_force;
-    a.fxk = s->fxk;
+    make_coeffs(s->tau, s->force, s->scale, &a.co);
     a.macro = s->macro;
     a.partial = s->partial;
     a.err = s->err;
@@ -892,7 +897,7 @@ int plb_step_async(plb_sim *s, int it_begin, int nsteps)
     for (int k = 0; k < nsteps; k++) {
         a.fin = s->f[s->cur];
         a.fout = s->f[s->cur ^ 1];
-        a.it = it_begin + k;
+        a.co.it = it_begin + k;
         const bool last = (k == nsteps - 1);
         cudaError_t e = launch_step(s->precision, last, a, s->block, s->stream);
         if (e != cudaSuccess) {

@@ -45,14 +45,13 @@ template <typename T>
 __device__ __forceinline__ T ldg_t(const T *p) { return __ldg(p); }
 
 template <typename T>
-__device__ __forceinline__ void gather(const StepArgs &a, int i, T (&f)[Q])
+__device__ __forceinline__ void gather(const T *fin, const uint32_t *nbr,
+                                       long long np, long long i, T (&f)[Q])
 {
-    const T *fin = (const T *)a.fin;
-    const long long np = a.npad;
     f[0] = ldg_t(fin + i);
 #pragma unroll
     for (int j = 1; j < Q; j++) {
-        const uint32_t w = __ldcs(a.nbr + (long long)(j - 1) * np + i);
+        const uint32_t w = __ldcs(nbr + (long long)(j - 1) * np + i);
         const T *p = (w & kBounce) ? fin + (long long)opp(j) * np + i
                                    : fin + (long long)j * np + (w & kSrcMask);
         f[j] = ldg_t(p);
@@ -109,7 +108,7 @@ struct Macro {
 };
 
 __device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
-                                                     const StepArgs &a)
+                                                     const Coeffs &a)
 {
     Macro m;
     double rho = f[0];
@@ -170,7 +169,7 @@ __device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
 /* ------------------------------------------------------ FP64 with FMA */
 
 __device__ __forceinline__ Macro collide_fp64_fma(double (&f)[Q],
-                                                   const StepArgs &a)
+                                                   const Coeffs &a)
 {
     Macro m;
     double s[Q], d[Q];
@@ -226,7 +225,7 @@ __device__ __forceinline__ Macro collide_fp64_fma(double (&f)[Q],
  * becomes, exactly in real arithmetic,
  *   g'_j = (1-omega) g_j + omega delta + rho ((omega + a_j) P_j + a_j),
  * which keeps every FP32 quantity at deviation scale. */
-__device__ __forceinline__ Macro collide_dev32(float (&g)[Q], const StepArgs &a)
+__device__ __forceinline__ Macro collide_dev32(float (&g)[Q], const Coeffs &a)
 {
     Macro m;
     float d[Q];
@@ -293,7 +292,7 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float
 /* ----------------------------------------- FP64 on the integer pipes */
 
 template <bool MACRO>
-__device__ __forceinline__ Macro collide_fx(double (&f)[Q], const StepArgs &a,
+__device__ __forceinline__ Macro collide_fx(double (&f)[Q], const Coeffs &a,
                                             bool &fallback)
 {
     uint64_t b[Q];
@@ -327,56 +326,74 @@ template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
 template <int PREC> struct MinBlocks { static constexpr int v = 1; };
 template <> struct MinBlocks<PLB_FP64> { static constexpr int v = 2; };
 
+/* Gather, collide and store node i.  Returns the macros; *dev_max receives
+ * the largest stored deviation magnitude of the 16-bit forms. */
+template <int PREC, bool MACRO>
+__device__ __forceinline__ Macro step_node(const void *fin_, void *fout_,
+                                           const uint32_t *nbr, long long np,
+                                           long long i, const Coeffs &co,
+                                           unsigned int &flags, float &dev_max)
+{
+    using T = typename StoreOf<PREC>::T;
+    const T *fin = (const T *)fin_;
+    T *fout = (T *)fout_;
+    T raw[Q];
+    gather<T>(fin, nbr, np, i, raw);
+    Macro m;
+    if constexpr (PREC == PLB_FP64) {
+        bool fallback;
+        m = collide_fx<MACRO>(raw, co, fallback);
+        if (fallback) {
+            /* outside the fixed-point range: native FP64 from the streamed
+             * values, gathered again */
+            gather<T>(fin, nbr, np, i, raw);
+            m = collide_fp64_fma(raw, co);
+            flags |= 2u;
+        }
+#pragma unroll
+        for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
+    } else if constexpr (PREC == PLB_FP64_EXACT || PREC == PLB_FP64_FMA) {
+        if constexpr (PREC == PLB_FP64_EXACT) m = collide_fp64_exact(raw, co);
+        else m = collide_fp64_fma(raw, co);
+#pragma unroll
+        for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
+    } else {
+        float g[Q];
+#pragma unroll
+        for (int j = 0; j < Q; j++) g[j] = to_f(raw[j]) * co.inv_scale;
+        m = collide_dev32(g, co);
+        float big = 0.f;
+#pragma unroll
+        for (int j = 0; j < Q; j++) {
+            const float h = g[j] * co.scale;
+            big = fmaxf(big, fabsf(h));
+            fout[(long long)j * np + i] = from_f<T>(h);
+        }
+        if (PREC == PLB_FP16DEV && !(big <= 60000.f)) flags |= 1u;
+        dev_max = big;
+    }
+    return m;
+}
+
 template <int PREC, bool MACRO>
 __global__ void __launch_bounds__(256, MinBlocks<PREC>::v)
 k_step(const StepArgs a)
 {
-    using T = typename StoreOf<PREC>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double sum_u = 0.0, sum_r = 0.0;
     if (i < a.n) {
-        T raw[Q];
-        gather<T>(a, i, raw);
-        Macro m;
-        T *fout = (T *)a.fout;
-        const long long np = a.npad;
-        if constexpr (PREC == PLB_FP64) {
-            bool fallback;
-            m = collide_fx<MACRO>(raw, a, fallback);
-            if (fallback) {
-                /* outside the fixed-point range: native FP64 from the
-                 * streamed values, gathered again */
-                gather<double>(a, i, raw);
-                m = collide_fp64_fma(raw, a);
-                atomicOr(a.flags, 2u);
-            }
-#pragma unroll
-            for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
-        } else if constexpr (PREC == PLB_FP64_EXACT || PREC == PLB_FP64_FMA) {
-            if constexpr (PREC == PLB_FP64_EXACT) m = collide_fp64_exact(raw, a);
-            else m = collide_fp64_fma(raw, a);
-#pragma unroll
-            for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
-        } else {
-            float g[Q];
-#pragma unroll
-            for (int j = 0; j < Q; j++) g[j] = to_f(raw[j]) * a.inv_scale;
-            m = collide_dev32(g, a);
-            float big = 0.f;
-#pragma unroll
-            for (int j = 0; j < Q; j++) {
-                const float h = g[j] * a.scale;
-                big = fmaxf(big, fabsf(h));
-                fout[(long long)j * np + i] = from_f<T>(h);
-            }
-            if (PREC == PLB_FP16DEV && !(big <= 60000.f)) atomicOr(a.flags, 1u);
-        }
+        float dm = 0.f;
+        unsigned int fl = 0;
+        const Macro m = step_node<PREC, MACRO>(a.fin, a.fout, a.nbr, a.npad, i, a.co,
+                                               fl, dm);
+        if (fl) atomicOr(a.flags, fl);
         if (m.bad) {
             const unsigned long long key =
-                ((unsigned long long)(unsigned)a.it << 32) | (unsigned)a.perm[i];
+                ((unsigned long long)(unsigned)a.co.it << 32) | (unsigned)a.perm[i];
             atomicMin(a.err, key);
         }
         if (MACRO) {
+            const long long np = a.npad;
             a.macro[i] = m.rho;
             a.macro[np + i] = m.u;
             a.macro[2 * np + i] = m.v;
@@ -404,6 +421,64 @@ k_step(const StepArgs a)
     }
 }
 
+/* Batch step: block b belongs to sample blk_sample[b] (or is free). */
+template <int PREC, bool MACRO>
+__global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC>::v)
+k_batch_step(const BatchArgs a)
+{
+    const int s = a.blk_sample[blockIdx.x];
+    double sum_u = 0.0, sum_r = 0.0;
+    float dmax = 0.f;
+    if (s >= 0) {
+        const SampleDev &sp = a.samples[s];
+        const long long i = (long long)blockIdx.x * kBatchBlock + threadIdx.x;
+        if (i - sp.base < sp.n) {
+            Coeffs co = sp.co;
+            co.it = *a.t_base + a.t_off - sp.start;
+            unsigned int fl = 0;
+            const Macro m = step_node<PREC, MACRO>(a.fin, a.fout, a.nbr, a.npad, i, co,
+                                                   fl, dmax);
+            if (fl | (m.bad ? 4u : 0u)) atomicOr(a.serr + s, fl | (m.bad ? 4u : 0u));
+            if (MACRO) {
+                const long long np = a.npad;
+                if (a.macro) {
+                    a.macro[i] = m.rho;
+                    a.macro[np + i] = m.u;
+                    a.macro[2 * np + i] = m.v;
+                    a.macro[3 * np + i] = m.w;
+                }
+                sum_u = m.u;
+                sum_r = m.rho;
+            }
+        }
+    }
+    if (MACRO) {
+        __shared__ double su[32], sr[32];
+        __shared__ float sd[32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sum_u += __shfl_down_sync(0xffffffffu, sum_u, o);
+            sum_r += __shfl_down_sync(0xffffffffu, sum_r, o);
+            dmax = fmaxf(dmax, __shfl_down_sync(0xffffffffu, dmax, o));
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) { su[wid] = sum_u; sr[wid] = sum_r; sd[wid] = dmax; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tu = 0.0, tr = 0.0;
+            float td = 0.f;
+            for (int k = 0; k < kBatchBlock / 32; k++) {
+                tu += su[k];
+                tr += sr[k];
+                td = fmaxf(td, sd[k]);
+            }
+            a.partial[blockIdx.x] = tu;
+            a.partial[gridDim.x + blockIdx.x] = tr;
+            a.partial[2 * gridDim.x + blockIdx.x] = (double)td;
+        }
+    }
+}
+
 template <int PREC>
 static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
                                cudaStream_t s)
@@ -413,6 +488,30 @@ static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
     if (macros) k_step<PREC, true><<<grid, block, 0, s>>>(a);
     else k_step<PREC, false><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int PREC>
+static cudaError_t launch_batch_prec(bool macros, const BatchArgs &a, int nb,
+                                     cudaStream_t s)
+{
+    if (nb == 0) return cudaSuccess;
+    if (macros) k_batch_step<PREC, true><<<nb, kBatchBlock, 0, s>>>(a);
+    else k_batch_step<PREC, false><<<nb, kBatchBlock, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_step(int precision, bool macros, const BatchArgs &a,
+                              int nblocks, cudaStream_t s)
+{
+    switch (precision) {
+    case PLB_FP64_EXACT: return launch_batch_prec<PLB_FP64_EXACT>(macros, a, nblocks, s);
+    case PLB_FP64: return launch_batch_prec<PLB_FP64>(macros, a, nblocks, s);
+    case PLB_FP64_FMA: return launch_batch_prec<PLB_FP64_FMA>(macros, a, nblocks, s);
+    case PLB_FP32: return launch_batch_prec<PLB_FP32>(macros, a, nblocks, s);
+    case PLB_FP16DEV: return launch_batch_prec<PLB_FP16DEV>(macros, a, nblocks, s);
+    case PLB_BF16DEV: return launch_batch_prec<PLB_BF16DEV>(macros, a, nblocks, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,

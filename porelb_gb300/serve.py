@@ -1,0 +1,95 @@
+"""Permeability-solve server with continuous batching.
+
+Requests (geometry seed and size, porosity, sphere radius, tau, force,
+tolerance) arrive over time.  The server keeps one device node pool (a
+``Batch``) sized from an HBM budget; at every interval boundary it admits
+waiting requests that fit (first come first served, with smaller requests
+allowed to pass a head that does not fit), builds their geometry and node
+table on the device, advances every resident sample by one interval (K
+lattice steps in one CUDA-graph replay), and retires converged samples,
+whose blocks the next admissions reuse.  Work of requests that arrived while
+others run overlaps on the device with theirs.
+
+Latency of a request = completion time - arrival time (wall clock).
+"""
+import time
+
+import numpy as np
+
+from .batch import Batch
+
+
+class Server:
+    def __init__(self, hbm_budget_bytes, precision="fp16dev", check_every=500,
+                 max_samples=4096, device=0, lookahead=64):
+        bpn = Batch.bytes_per_node(precision)
+        self.capacity = int(hbm_budget_bytes // bpn)
+        self.batch = Batch(self.capacity, max_samples, precision, check_every,
+                           device=device)
+        self.precision = precision
+        self.lookahead = lookahead
+
+    def close(self):
+        self.batch.close()
+
+    def serve(self, requests, time_scale=1.0, max_wall=None):
+        """Serve requests (objects with .arrival in seconds, .edge, .seed,
+        .porosity, .rmin, .rmax, .tau, .force, .tol) in real time.  Returns a
+        list of per-request records and a summary."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        waiting = []
+        live = {}
+        done = []
+        t0 = time.perf_counter()
+        node_steps = 0
+        intervals = 0
+        K = self.batch.check_every
+        while pending or waiting or live:
+            now = time.perf_counter() - t0
+            if max_wall is not None and now > max_wall:
+                break
+            while pending and pending[0].arrival * time_scale <= now:
+                waiting.append(pending.pop(0))
+            # admission: FCFS with bounded lookahead past a head that does
+            # not fit into the free node ranges
+            admitted = []
+            for r in waiting[: self.lookahead]:
+                sid = self.batch.try_add_packed(
+                    r.seed, r.edge, r.edge, r.edge, r.rmin, r.rmax, r.porosity,
+                    r.tau, r.force, tol=r.tol)
+                if sid is not None:
+                    live[sid] = dict(req=r, admitted=time.perf_counter() - t0,
+                                     nodes=self.batch.num_nodes(sid))
+                    admitted.append(r)
+            for r in admitted:
+                waiting.remove(r)
+            if not live:
+                if pending:
+                    time.sleep(max(0.0, pending[0].arrival * time_scale -
+                                   (time.perf_counter() - t0)))
+                continue
+            node_steps += sum(v["nodes"] for v in live.values()) * K
+            self.batch.run(1)
+            intervals += 1
+            for sid in self.batch.poll():
+                res = self.batch.result(sid)
+                v = live.pop(sid)
+                end = time.perf_counter() - t0
+                r = v["req"]
+                done.append(dict(index=r.index, edge=r.edge, nodes=v["nodes"],
+                                 arrival=r.arrival * time_scale,
+                                 admitted=v["admitted"], finished=end,
+                                 latency=end - r.arrival * time_scale,
+                                 steps=res["steps"], k_darcy=res["k_darcy"],
+                                 status=res["status"], tau=r.tau, tol=r.tol))
+                self.batch.release(sid)
+        wall = time.perf_counter() - t0
+        lat = np.array([d["latency"] for d in done]) if done else np.zeros(1)
+        summary = dict(requests=len(done), wall_s=wall,
+                       solves_per_s=len(done) / wall if wall > 0 else 0.0,
+                       p50_latency_s=float(np.percentile(lat, 50)),
+                       p99_latency_s=float(np.percentile(lat, 99)),
+                       fluid_mlups=node_steps / wall / 1e6 if wall > 0 else 0.0,
+                       intervals=intervals, capacity_nodes=self.capacity,
+                       precision=self.precision, check_every=K)
+        return done, summary
