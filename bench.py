@@ -304,6 +304,165 @@ def run_gpu(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------- batched / served
+
+def _steady_batch(samples, precision, K, max_steps, capacity=None):
+    """Run samples (workloads.Sample) to steady state in one pool; returns
+    {index: result}, node-steps and wall time."""
+    import porelb_gb300 as P  # noqa: F401
+    from porelb_gb300.batch import Batch
+    cap = capacity or sum(int(s.edge ** 3 * s.porosity * 1.05) + 512
+                          for s in samples)
+    b = Batch(cap, max(len(samples), 1), precision, check_every=K)
+    ids = {}
+    for smp in samples:
+        sid = b.add_packed(smp.seed, smp.edge, smp.edge, smp.edge, smp.rmin,
+                           smp.rmax, smp.porosity, smp.tau, smp.force,
+                           tol=smp.tol, max_steps=max_steps)
+        ids[sid] = (smp.index, b.num_nodes(sid))
+    out = {}
+    node_steps = 0
+    t0 = time.perf_counter()
+    while True:
+        live = b.info()["used_nodes"]
+        if live == 0:
+            break
+        node_steps += sum(n for sid, (_, n) in ids.items()
+                          if b.result(sid)["status"] == 0) * K
+        if b.run(1) == 0:
+            pass
+        for sid in b.poll():
+            idx, n = ids[sid]
+            r = b.result(sid)
+            r["nodes"] = n
+            out[idx] = r
+    wall = time.perf_counter() - t0
+    b.close()
+    return out, node_steps, wall
+
+
+def run_batched(args):
+    import torch
+    import porelb_gb300 as P
+    from porelb_gb300.workloads import batched_samples
+    torch.cuda.set_device(0)
+    samples = batched_samples(args.samples, 3)
+    K = args.check_every
+    res32, ns32, wall32 = _steady_batch(samples, "fp32", K, args.max_steps)
+    res64, ns64, wall64 = _steady_batch(samples, "fp64", K, args.max_steps)
+    # plain kernel per sample (FP32), timed on a fixed step count, then the
+    # loop over samples is costed with each sample's own step count
+    loop_s = 0.0
+    for smp in samples:
+        sim = P.Simulation.packed(smp.seed, smp.edge, smp.edge, smp.edge,
+                                  smp.rmin, smp.rmax, smp.porosity,
+                                  tau=smp.tau, force=smp.force,
+                                  precision="fp32")
+        sim.init_dist_macro()
+        sim.step(20)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.step(args.plain_steps, it_begin=20)
+        el = time.perf_counter() - t0
+        sim.close()
+        loop_s += el / args.plain_steps * res32[smp.index]["steps"]
+    errs = [abs(res32[i]["k_darcy"] - res64[i]["k_darcy"]) /
+            abs(res64[i]["k_darcy"]) for i in res32 if res64[i]["k_darcy"]]
+    conv = sum(1 for r in res32.values() if r["status"] == 1)
+    line = {
+        "metric": "fluid MLUPS (batched, FP32)",
+        "value": round(ns32 / wall32 / 1e6, 1), "unit": "MLUPS",
+        "plain_loop_mlups": round(ns32 / loop_s / 1e6, 1),
+        "speedup_vs_plain_loop": round(loop_s / wall32, 3),
+        "fp64_batched_mlups": round(ns64 / wall64 / 1e6, 1),
+        "samples": len(samples), "converged": conv,
+        "k_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs)},
+        "wall_s": round(wall32, 2), "check_every": K,
+        "config": {"workload": "batched 64 samples, seed 3",
+                   "edges": [s.edge for s in samples],
+                   "tol": 1e-7, "force": 1e-6, "max_steps": args.max_steps},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_served(args):
+    import torch
+    from porelb_gb300.serve import Server
+    from porelb_gb300.workloads import serving_requests
+    torch.cuda.set_device(0)
+    reqs = serving_requests(args.requests, 4, args.rate)
+    srv = Server(args.budget_gb * 1e9, "fp16dev", check_every=args.check_every)
+    done, summ = srv.serve(reqs, max_wall=args.max_wall)
+    srv.close()
+    # FP64 plain form on a sample of the same requests, one at a time
+    sub = [r for r in reqs if any(d["index"] == r.index for d in done)][: args.fp64_check]
+    res64, ns64, wall64 = _steady_batch(sub, "fp64", args.check_every,
+                                        args.max_steps)
+    by = {d["index"]: d for d in done}
+    errs = [abs(by[i]["k_darcy"] - r["k_darcy"]) / abs(r["k_darcy"])
+            for i, r in res64.items() if r["k_darcy"]]
+    line = {
+        "metric": "perm solves/s (served, FP16 deviations)",
+        "value": round(summ["solves_per_s"], 3), "unit": "solves/s",
+        "p50_latency_s": round(summ["p50_latency_s"], 3),
+        "p99_latency_s": round(summ["p99_latency_s"], 3),
+        "fluid_mlups": round(summ["fluid_mlups"], 1),
+        "requests_done": summ["requests"], "requests": len(reqs),
+        "k_rel_err_vs_fp64": {"checked": len(errs),
+                              "max": max(errs) if errs else None,
+                              "median": statistics.median(errs) if errs else None},
+        "fp64_mlups_on_checked": round(ns64 / wall64 / 1e6, 1) if wall64 else None,
+        "config": {"workload": f"{len(reqs)} Poisson requests, seed 4",
+                   "rate_per_s": args.rate, "budget_gb": args.budget_gb,
+                   "check_every": args.check_every,
+                   "capacity_nodes": summ["capacity_nodes"]},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_precision(args):
+    """1024^3, porosity 0.20, R 8, seed 2, tau 0.9, F 5e-7 at three storage
+    forms (MLUPS), and k of the 256^3 corner subvolume at each form against
+    its FP64 solve."""
+    import torch
+    import porelb_gb300 as P
+    from porelb_gb300.workloads import Sample
+    torch.cuda.set_device(0)
+    n = args.edge
+    out = {}
+    for prec in ("fp64", "fp32", "fp16dev"):
+        sim = P.Simulation.packed(2, n, n, n, 8.0, 8.0, 0.20, tau=0.9,
+                                  force=5e-7, precision=prec)
+        sim.init_dist_macro()
+        sim.step(3)
+        stream = torch.cuda.ExternalStream(sim.stream, device=0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step_async(args.steps, it_begin=3)
+        e1.record(stream)
+        sim.sync()
+        ms = e0.elapsed_time(e1)
+        out[prec] = dict(mlups=round(sim.N * args.steps / (ms * 1e-3) / 1e6, 1),
+                         bytes_per_node=BYTES_PER_NODE[prec],
+                         num_node=sim.N, device_bytes=sim.info()["device_bytes"])
+        sim.close()
+    sub = Sample(0, 256, 0.20, 8.0, 8.0, 0.9, 5e-7, 1e-7, 2)
+    ks = {}
+    for prec in ("fp64", "fp32", "fp16dev"):
+        r, _, _ = _steady_batch([sub], prec, args.check_every, args.max_steps)
+        ks[prec] = r[0]
+    for prec in ("fp32", "fp16dev"):
+        out[prec]["k_rel_err_vs_fp64_256"] = abs(ks[prec]["k_darcy"] - ks["fp64"]["k_darcy"]) / abs(ks["fp64"]["k_darcy"])
+    line = {"metric": "fluid MLUPS by storage form", "unit": "MLUPS",
+            "value": out["fp16dev"]["mlups"], "forms": out,
+            "k_256": {p: ks[p]["k_darcy"] for p in ks},
+            "steps_256": {p: ks[p]["steps"] for p in ks},
+            "config": {"workload": f"{n}^3 sphere pack seed 2 R 8 porosity 0.20",
+                       "tau": 0.9, "force": 5e-7, "subvolume": "256^3 pack of the same parameters"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -317,7 +476,25 @@ def main():
     ap.add_argument("--e2e-reps", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mode", default="plain",
+                    choices=["plain", "batched", "served", "precision"])
+    ap.add_argument("--samples", type=int, default=64)
+    ap.add_argument("--check-every", type=int, default=1000)
+    ap.add_argument("--max-steps", type=int, default=200000)
+    ap.add_argument("--plain-steps", type=int, default=200)
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--rate", type=float, default=5.0)
+    ap.add_argument("--budget-gb", type=float, default=80.0)
+    ap.add_argument("--max-wall", type=float, default=None)
+    ap.add_argument("--fp64-check", type=int, default=32)
+    ap.add_argument("--edge", type=int, default=1024)
     args = ap.parse_args()
+    if args.mode == "batched":
+        return run_batched(args)
+    if args.mode == "served":
+        return run_served(args)
+    if args.mode == "precision":
+        return run_precision(args)
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORC_PATH = os.path.join(HERE, "liborc.so")
 REF_SOLVER_PATH = os.path.join(HERE, "_ref", "libref_porelb.so")
 REF_PRE_PATH = os.path.join(HERE, "_ref", "libref_pre.so")
+REF_POST_PATH = os.path.join(HERE, "_ref", "libref_post.so")
 
 Q = 19
 NB_DTYPE = np.dtype([("node_type", "u1"), ("pad_", "u1"),
@@ -225,6 +226,19 @@ def ref_write_vbin(flag, nx, ny, nz, num_p, path):
         flag.tofile(fp)
         return pre.ref_build_and_save_v(fp.encode(), nx, ny, nz, num_p,
                                         os.fsencode(path))
+
+
+def ref_postprocess(workdir, args):
+    """The reference postprocess main in workdir with argv args."""
+    if not os.path.exists(REF_POST_PATH):
+        raise ImportError("oracle/_ref/libref_post.so not built")
+    lib = ctypes.CDLL(REF_POST_PATH)
+    lib.ref_postprocess.restype = _I
+    lib.ref_postprocess.argtypes = [ctypes.c_char_p, _I,
+                                    ctypes.POINTER(ctypes.c_char_p)]
+    argv = ["postprocess.x"] + [str(a) for a in args]
+    arr = (ctypes.c_char_p * len(argv))(*[a.encode() for a in argv])
+    return lib.ref_postprocess(os.fsencode(workdir), len(argv), arr)
 
 
 def ref_run(workdir, num_ranks, it_max, tau=float("nan"),
