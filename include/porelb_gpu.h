@@ -76,6 +76,17 @@ enum {
 /* Node ordering in device memory. */
 enum { PLB_ORDER_MORTON = 0, PLB_ORDER_REFERENCE = 1 };
 
+/* Wall rule. */
+enum {
+    PLB_BOUNDARY_REFERENCE = 0, /* porelb's link bounce-back as written
+                                   (porelb.c:296-297): the bounced value lands
+                                   in f1[x][j] instead of f1[x][re j], so some
+                                   slots are written twice and others never */
+    PLB_BOUNDARY_HALFWAY = 1    /* standard half-way bounce-back: a population
+                                   that would stream into a solid cell returns
+                                   to its node reversed; conserves mass */
+};
+
 /* Halo semantics for tables written with num_p > 1. */
 enum {
     PLB_HALO_AUTO = -1,        /* REMOTE_WINS when num_p > 1, else SINGLE */
@@ -92,7 +103,8 @@ typedef struct {
     int halo;        /* PLB_HALO_* */
     int block_size;  /* threads per block for the step kernel; 0 = default */
     int device;      /* CUDA device ordinal */
-    int reserved[7];
+    int boundary;    /* PLB_BOUNDARY_REFERENCE (default) or PLB_BOUNDARY_HALFWAY */
+    int reserved[6];
 } plb_params;
 
 typedef struct plb_sim plb_sim;

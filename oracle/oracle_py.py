@@ -66,6 +66,7 @@ def orc():
         lib.orc_num_node.restype = _I
         lib.orc_num_node.argtypes = [_V]
         lib.orc_pull_table.argtypes = [_V, _I, _I, _IP, _I, _V, _V]
+        lib.orc_pull_table_rule.argtypes = [_V, _I, _I, _IP, _I, _I, _V, _V]
         lib.orc_pull_step.restype = _I
         lib.orc_pull_step.argtypes = [_V, _V, _I, _V, _V, _V, _V, _V, _V, _D,
                                       _D, _I, _IP]
@@ -169,21 +170,22 @@ class OracleSim:
             pass
 
 
-def pull_table(V, v_sub_start, remote_wins=False):
+def pull_table(V, v_sub_start, remote_wins=False, halfway=False):
     lib = orc()
     V = np.ascontiguousarray(V, dtype=NODE_DTYPE)
     vs = np.ascontiguousarray(v_sub_start, dtype=np.int32)
     kind = np.zeros(len(V) * 18, np.uint8)
     src = np.zeros(len(V) * 18, np.uint32)
-    lib.orc_pull_table(_p(V), len(V), len(vs), vs.ctypes.data_as(_IP),
-                       int(remote_wins), _p(kind), _p(src))
+    lib.orc_pull_table_rule(_p(V), len(V), len(vs), vs.ctypes.data_as(_IP),
+                            int(remote_wins), int(halfway), _p(kind), _p(src))
     return kind, src
 
 
-def pull_run(V, v_sub_start, tau, force, nsteps, remote_wins=False):
+def pull_run(V, v_sub_start, tau, force, nsteps, remote_wins=False,
+             halfway=False):
     """Pull-form restatement from rest: returns (f0, f1, macros)."""
     lib = orc()
-    kind, src = pull_table(V, v_sub_start, remote_wins)
+    kind, src = pull_table(V, v_sub_start, remote_wins, halfway)
     N = len(V)
     w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
     f0 = np.tile(w, N).astype(np.float64)

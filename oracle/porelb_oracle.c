@@ -20,7 +20,7 @@
  * boundary is applied after every rank's local stream, as the reference's
  * MPI_Waitall + update_recv_dist order makes it (porelb.c:428-433).
  *
- * Parity pin: tests/test_oracle_vs_reference.py compares this file with the
+ * Parity pin: tests/test_oracle.py compares this file with the
  * reference compiled from its own sources (oracle/_ref/), byte for byte.
  */
 #include "porelb_oracle.h"
@@ -420,6 +420,16 @@ void orc_pull_table(const plb_node_info *V, int num_node, int num_p,
                     const int *v_sub_start, int remote_wins, uint8_t *kind,
                     uint32_t *src)
 {
+    orc_pull_table_rule(V, num_node, num_p, v_sub_start, remote_wins, 0, kind, src);
+}
+
+/* halfway != 0: the standard half-way bounce-back instead of the
+ * reference's rule: pull from s when s is fluid, else the node's own
+ * reversed population. */
+void orc_pull_table_rule(const plb_node_info *V, int num_node, int num_p,
+                         const int *v_sub_start, int remote_wins, int halfway,
+                         uint8_t *kind, uint32_t *src)
+{
     int *start = (int *)calloc((size_t)num_p + 1, sizeof(int));
     for (int p = 0; p < num_p; p++) start[p] = v_sub_start ? v_sub_start[p] : 0;
     start[num_p] = num_node;
@@ -436,7 +446,8 @@ void orc_pull_table(const plb_node_info *V, int num_node, int num_p,
             else if (sn.node_type == PLB_TYPE_EXTERN)
                 sg = (long)start[sn.node_pid] + sn.node_id;
             uint8_t k;
-            if (push && !bounce) k = 0;
+            if (halfway) k = push ? 0 : 1;
+            else if (push && !bounce) k = 0;
             else if (!push && bounce) k = 1;
             else if (!push && !bounce) k = 2;
             else if (remote_wins && sn.node_type == PLB_TYPE_EXTERN) k = 0;

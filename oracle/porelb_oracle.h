@@ -7,7 +7,7 @@
  *
  * Parity pin: every function here is checked bit-exactly against the
  * reference itself, compiled from its own sources by oracle/Makefile into
- * oracle/_ref/ (tests/test_oracle_vs_reference.py), and the committed golden
+ * oracle/_ref/ (tests/test_oracle.py), and the committed golden
  * fixtures in tests/golden/ were written by that compiled reference.
  */
 #ifndef PORELB_ORACLE_H_
@@ -55,6 +55,12 @@ int orc_num_node(orc_sim *s);
 void orc_pull_table(const plb_node_info *V, int num_node, int num_p,
                     const int *v_sub_start, int remote_wins, uint8_t *kind,
                     uint32_t *src);
+/* As orc_pull_table; halfway != 0 gives the standard half-way bounce-back
+ * (every slot written once: pull from s if fluid, else f0[i][re j]). */
+void orc_pull_table_rule(const plb_node_info *V, int num_node, int num_p,
+                         const int *v_sub_start, int remote_wins, int halfway,
+                         uint8_t *kind, uint32_t *src);
+
 /* One fused pull-stream + collide step on AoS arrays using that table:
  * f1 := stream(f0) (kind 2 slots untouched), then collide f1 -> f0. */
 int orc_pull_step(const uint8_t *kind, const uint32_t *src, int num_node,

@@ -30,13 +30,15 @@ ERR_NOMEM, ERR_DENSITY, ERR_NUMP, ERR_STATE = -5, -6, -7, -8
 FP64_EXACT, FP64, FP32, FP16DEV, BF16DEV, FP64_FMA = 0, 1, 2, 3, 4, 5
 ORDER_MORTON, ORDER_REFERENCE = 0, 1
 HALO_AUTO, HALO_SINGLE, HALO_REMOTE_WINS = -1, 0, 1
+BOUNDARY_REFERENCE, BOUNDARY_HALFWAY = 0, 1
 
 
 class Params(ctypes.Structure):
     _fields_ = [("tau", ctypes.c_double), ("force_x", ctypes.c_double),
                 ("precision", ctypes.c_int), ("ordering", ctypes.c_int),
                 ("halo", ctypes.c_int), ("block_size", ctypes.c_int),
-                ("device", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("device", ctypes.c_int), ("boundary", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
 
 
 class SampleParams(ctypes.Structure):

@@ -23,6 +23,8 @@ PRECISIONS = {"fp64_exact": _lib.FP64_EXACT, "fp64": _lib.FP64,
 ORDERINGS = {"morton": _lib.ORDER_MORTON, "reference": _lib.ORDER_REFERENCE}
 HALOS = {"auto": _lib.HALO_AUTO, "single": _lib.HALO_SINGLE,
          "remote_wins": _lib.HALO_REMOTE_WINS}
+BOUNDARIES = {"reference": _lib.BOUNDARY_REFERENCE,
+              "halfway": _lib.BOUNDARY_HALFWAY}
 
 
 class PorelbError(RuntimeError):
@@ -121,7 +123,8 @@ def sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, device=0):
     return flag, ns.value, phi.value
 
 
-def _params(tau, force, precision, ordering, halo, block_size, device):
+def _params(tau, force, precision, ordering, halo, block_size, device,
+            boundary="reference"):
     lib = _lib.load()
     p = _lib.Params()
     lib.plb_default_params(ctypes.byref(p))
@@ -131,6 +134,7 @@ def _params(tau, force, precision, ordering, halo, block_size, device):
     p.halo = HALOS[halo]
     p.block_size = block_size
     p.device = device
+    p.boundary = BOUNDARIES[boundary]
     return p
 
 
@@ -141,7 +145,7 @@ class Simulation:
 
     def __init__(self, V, nx, ny, nz, v_sub_start=None, tau=0.8,
                  force=1e-3, precision="fp64_exact", ordering="morton",
-                 halo="auto", block_size=0, device=0):
+                 halo="auto", block_size=0, device=0, boundary="reference"):
         self._lib = _lib.load()
         self.V = np.ascontiguousarray(V, dtype=NODE_DTYPE)
         self.nx, self.ny, self.nz = nx, ny, nz
@@ -150,14 +154,8 @@ class Simulation:
         self.num_p = len(self.v_sub_start)
         self.tau, self.force = float(tau), float(force)
         self.precision = precision
-        p = _lib.Params()
-        self._lib.plb_default_params(ctypes.byref(p))
-        p.tau, p.force_x = self.tau, self.force
-        p.precision = PRECISIONS[precision]
-        p.ordering = ORDERINGS[ordering]
-        p.halo = HALOS[halo]
-        p.block_size = block_size
-        p.device = device
+        p = _params(tau, force, precision, ordering, halo, block_size, device,
+                    boundary)
         h = ctypes.c_void_p()
         _check(self._lib.plb_create(_ptr(self.V), len(self.V), nx, ny, nz,
                                     self.num_p, _iptr(self.v_sub_start),
@@ -258,13 +256,14 @@ class Simulation:
     @classmethod
     def from_flag(cls, flag, nx, ny, nz, num_p=1, tau=0.8, force=1e-3,
                   precision="fp64_exact", ordering="morton", halo="auto",
-                  block_size=0, device=0):
+                  block_size=0, device=0, boundary="reference"):
         """build_V + create on the device from a 0/1 flag grid."""
         lib = _lib.load()
         flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
         if flag.size != nx * ny * nz:
             raise ValueError("flag size does not match nx*ny*nz")
-        p = _params(tau, force, precision, ordering, halo, block_size, device)
+        p = _params(tau, force, precision, ordering, halo, block_size, device,
+                    boundary)
         h = ctypes.c_void_p()
         _check(lib.plb_create_from_flag(_ptr(flag), nx, ny, nz, num_p,
                                         ctypes.byref(p), ctypes.byref(h)),
@@ -274,10 +273,11 @@ class Simulation:
     @classmethod
     def packed(cls, seed, nx, ny, nz, rmin, rmax, porosity, num_p=1, tau=0.8,
                force=1e-3, precision="fp64", ordering="morton", halo="auto",
-               block_size=0, device=0):
+               block_size=0, device=0, boundary="reference"):
         """Sphere pack, table and handle, all built on the device."""
         lib = _lib.load()
-        p = _params(tau, force, precision, ordering, halo, block_size, device)
+        p = _params(tau, force, precision, ordering, halo, block_size, device,
+                    boundary)
         h = ctypes.c_void_p()
         ns = ctypes.c_int(0)
         phi = ctypes.c_double(0.0)

@@ -393,7 +393,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     }
     if (rc == PLB_OK) {
         const long long base = blk0 * B;
-        rc = flag_tables(dflag, nx, ny, nz, 1, PLB_ORDER_MORTON, 0, lexbits, lexoffs, n,
+        rc = flag_tables(dflag, nx, ny, nz, 1, PLB_ORDER_MORTON, 0, 0, lexbits, lexoffs, n,
                          b->npad, b->perm + base, b->coord + base, b->nbr + base,
                          (uint32_t)base, (uint32_t)b->rest, b->st);
         if (rc != PLB_OK) free_range(b, blk0, nblk);

@@ -117,7 +117,7 @@ __global__ void k_assign_from_flag(const uint32_t *lexbits, const uint32_t *lexo
  * when s lies in another rank slab and remote_wins is set. */
 __global__ void k_nbr_from_flag(const uint32_t *lexbits, const uint32_t *obits,
                                 const uint32_t *ooffs, Grid g, int slab,
-                                int remote_wins, int n, long long npad,
+                                int remote_wins, int halfway, int n, long long npad,
                                 uint32_t word_base, uint32_t rest_word,
                                 const uint16_t *coord, uint32_t *nbr)
 {
@@ -141,7 +141,10 @@ __global__ void k_nbr_from_flag(const uint32_t *lexbits, const uint32_t *obits,
         const bool bounce = !bit_at(lexbits, ct);
         const bool remote = remote_wins && (sz / slab != z / slab);
         uint32_t word;
-        if (push && (!bounce || remote || cs > cx))
+        if (halfway)
+            word = push ? word_base + rank_in(obits, ooffs, device_key(g, sx, sy, sz))
+                        : kBounce;
+        else if (push && (!bounce || remote || cs > cx))
             word = word_base + rank_in(obits, ooffs, device_key(g, sx, sy, sz));
         else if (bounce)
             word = kBounce;
@@ -383,7 +386,7 @@ done:
 /* Morton (or reference) order, permutation, coordinates and pull table of
  * the fluid cells of a device flag grid, ranked by flag_rank. */
 int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
-                int ordering, int remote_wins, const uint32_t *lexbits,
+                int ordering, int remote_wins, int halfway, const uint32_t *lexbits,
                 const uint32_t *lexoffs, int n, long long npad, int *perm,
                 uint16_t *coord, uint32_t *nbr, uint32_t word_base,
                 uint32_t rest_word, cudaStream_t st)
@@ -413,8 +416,8 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
                                                        cells, n, npad, perm, coord);
     CKG(cudaGetLastError());
     k_nbr_from_flag<<<gsz((size_t)n, 128), 128, 0, st>>>(lexbits, obits, ooffs, g, nz / num_p,
-                                                        remote_wins, n, npad, word_base,
-                                                        rest_word, coord, nbr);
+                                                        remote_wins, halfway, n, npad,
+                                                        word_base, rest_word, coord, nbr);
     CKG(cudaGetLastError());
     CKG(cudaStreamSynchronize(st));
 done:

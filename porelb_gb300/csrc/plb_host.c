@@ -31,6 +31,7 @@ void plb_default_params(plb_params *p)
     p->halo = PLB_HALO_AUTO;
     p->block_size = 0;
     p->device = 0;
+    p->boundary = PLB_BOUNDARY_REFERENCE;
 }
 
 const char *plb_status_string(int s)

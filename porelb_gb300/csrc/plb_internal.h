@@ -108,7 +108,7 @@ int flag_rank(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
               uint32_t *lexbits, uint32_t *lexoffs, int *n, int *slab_start,
               cudaStream_t st);
 int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
-                int ordering, int remote_wins, const uint32_t *lexbits,
+                int ordering, int remote_wins, int halfway, const uint32_t *lexbits,
                 const uint32_t *lexoffs, int n, long long npad, int *perm,
                 uint16_t *coord, uint32_t *nbr, uint32_t word_base,
                 uint32_t rest_word, cudaStream_t st);

@@ -26,7 +26,7 @@ extern "C" void plb_host_constants(double tau, double force, double *omega,
 struct plb_sim {
     int n, nx, ny, nz, num_p;
     long long npad;
-    int precision, ordering, halo, block;
+    int precision, ordering, halo, block, boundary;
     int device;
     cudaStream_t stream;
     void *f[2];
@@ -283,7 +283,7 @@ __global__ void k_identity(int *perm, int *inv, int n)
  * nobody writes keeps its initial value: it reads the rest slot n. */
 __global__ void k_build_nbr(const plb_node_info *V, const int *perm,
                             const int *inv, const int *start, int num_p,
-                            int n, long long npad, int remote_wins,
+                            int n, long long npad, int remote_wins, int halfway,
                             uint32_t *nbr, uint16_t *coord, unsigned *bad)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -331,7 +331,9 @@ __global__ void k_build_nbr(const plb_node_info *V, const int *perm,
             }
         }
         uint32_t word;
-        if (push && (!bounce || (remote_wins && ext) || sg > i))
+        if (halfway)  /* standard rule: pull from s, or bounce if s is solid */
+            word = push ? (uint32_t)inv[sg] : kBounce;
+        else if (push && (!bounce || (remote_wins && ext) || sg > i))
             word = (uint32_t)inv[sg];
         else if (bounce)
             word = kBounce;
@@ -584,7 +586,8 @@ static int build_tables(plb_sim *s, const plb_node_info *V_host)
         const int remote_wins = (s->halo == PLB_HALO_REMOTE_WINS) ||
                                 (s->halo == PLB_HALO_AUTO && s->num_p > 1);
         k_build_nbr<<<nblk(n, 128), 128, 0, st>>>(dV, s->perm, inv, dstart, s->num_p, n,
-                                                 s->npad, remote_wins, s->nbr, s->coord, bad);
+                                                 s->npad, remote_wins, s->boundary,
+                                                 s->nbr, s->coord, bad);
         CKT(cudaGetLastError());
     }
     {
@@ -619,6 +622,7 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     if (n < 0 || nx <= 0 || ny <= 0 || nz <= 0 || num_p <= 0 || !v_sub_start ||
         !(p->tau > 0.5) || !isfinite(p->force_x) || elem_size(p->precision) == 0 ||
         (p->ordering != PLB_ORDER_MORTON && p->ordering != PLB_ORDER_REFERENCE) ||
+        (p->boundary != PLB_BOUNDARY_REFERENCE && p->boundary != PLB_BOUNDARY_HALFWAY) ||
         n >= (int)kSrcMask)
         return PLB_ERR_ARG;
     if (v_sub_start[0] != 0) return PLB_ERR_NUMP;
@@ -642,6 +646,7 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->precision = p->precision;
     s->ordering = p->ordering;
     s->halo = p->halo;
+    s->boundary = p->boundary;
     s->block = p->block_size > 0 ? p->block_size : 256;
     if (s->block > 256 || (s->block & 31)) s->block = 256;
     s->device = p->device;
@@ -738,9 +743,9 @@ static int create_from_dflag(const uint8_t *dflag, int nx, int ny, int nz,
     if (rc == PLB_OK) {
         const int remote_wins = (s->halo == PLB_HALO_REMOTE_WINS) ||
                                 (s->halo == PLB_HALO_AUTO && s->num_p > 1);
-        rc = flag_tables(dflag, nx, ny, nz, num_p, s->ordering, remote_wins, lexbits,
-                         lexoffs, n, s->npad, s->perm, s->coord, s->nbr, 0u,
-                         (uint32_t)n, st);
+        rc = flag_tables(dflag, nx, ny, nz, num_p, s->ordering, remote_wins,
+                         s->boundary, lexbits, lexoffs, n, s->npad, s->perm, s->coord,
+                         s->nbr, 0u, (uint32_t)n, st);
         rc = sim_finish(s, rc, out);
     }
     cudaFree(lexbits);
