@@ -54,6 +54,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device="cuda"):
+    """Largest value of x over the ranks (the step time the job takes)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def hbm_peak():
     try:
         with open(PEAKS) as fh:
@@ -229,12 +240,7 @@ def run_gpu(args, rank, world, local):
         sim.sync()
         barrier()
     it += args.steps
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
     ms_step = ms / args.steps
     value = N * args.steps * world / (ms * 1e-3) / 1e6
     kd, _ = sim.permeability()
@@ -258,7 +264,12 @@ def run_gpu(args, rank, world, local):
         el = time.perf_counter() - t0
         if k > 0:
             e2e_vals.append(N * e2e_steps / el / 1e6)
-    e2e = statistics.median(e2e_vals) * world if e2e_vals else None
+    if e2e_vals:
+        # whole-job rate: the slowest rank's time for the same per-rank work
+        t_rank = N * e2e_steps / (statistics.median(e2e_vals) * 1e6)
+        e2e = N * e2e_steps * world / max_over_ranks(t_rank, world) / 1e6
+    else:
+        e2e = None
 
     peak, peak_kind = hbm_peak()
     bpn = BYTES_PER_NODE[prec]

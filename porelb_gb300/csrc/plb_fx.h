@@ -23,9 +23,13 @@
  * with c = 3 (1 - w/2) F and w_j the lattice weights.  Every term is exact
  * algebra of the reference's expression.
  *
- * Range: the fast path requires f_0 in [2^-8, 1) and f_j in [2^-8, 1/4)
- * for j > 0, rho in [0.5, 1.2], and results in [2^-8, 8).  A node outside
- * that range is flagged and the caller recomputes it in native FP64.
+ * Range: collide<false> requires f_0 in [2^-8, 1) and f_j in [2^-8, 1/4)
+ * for j > 0, rho in [0.5, 1.2], and results in [2^-8, 8); collide<true>
+ * (constant shifts) requires every f_j, in and out, to stay in the binade of
+ * its weight: f_0 in [1/4, 1/2), f_1..6 in [1/32, 1/16), f_7..18 in
+ * [1/64, 1/32), i.e. deviations within -25%..+50% and -43%..+12.5% of the
+ * weights.  A node outside the range is flagged and the caller recomputes it
+ * in native FP64.
  *
  * The functions are host+device so that a CPU build of the same code checks
  * the integer algorithm bit for bit against the GPU.
@@ -144,6 +148,28 @@ FX_HD uint64_t to_bits(int64_t F, uint32_t &rmax_seen)
     return ((uint64_t)(ef + 867u) << 52) + q;
 }
 
+/* Fixed-binade forms: the value's biased FP64 exponent is E, the exponent
+ * of its lattice weight (1/3 -> 1021, 1/18 -> 1018, 1/36 -> 1017), so every
+ * shift is a constant.  A value outside that binade (input or result) sets
+ * *bad and the whole node is recomputed by the caller. */
+template <uint32_t E>
+FX_HD int64_t from_bits_fixed(uint64_t b, uint32_t &bad)
+{
+    bad |= (uint32_t)((uint32_t)(b >> 52) != E); /* also catches the sign bit */
+    const uint64_t m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+    return (int64_t)(m << (E - 1015u));
+}
+
+template <uint32_t E>
+FX_HD uint64_t to_bits_fixed(int64_t F, uint32_t &bad)
+{
+    constexpr uint32_t r = E - 1015u; /* bits below the 53-bit mantissa */
+    const uint64_t u = (uint64_t)F;
+    const uint64_t q = (u + ((uint64_t)1 << r >> 1)) >> r;
+    bad |= (uint32_t)((q >> 52) != 1u);
+    return ((uint64_t)(E - 1u) << 52) + q;
+}
+
 /* Q60 of a positive normal float in [2^-8, 4) */
 FX_HD int64_t from_float(float x)
 {
@@ -220,14 +246,23 @@ FX_HD float rcp_rn(float x)
  * FP64, kDensity if the density guard trips.  mom receives rho*2^60, the
  * shifted momentum and 1/rho for the macro output.
  */
+template <bool FIXED>
 FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
                        Moments &mom)
 {
-    uint32_t s0 = 0, s12 = 0, rmax = 0;
+    uint32_t s0 = 0, s12 = 0, rmax = 0, fbad = 0;
     int64_t F[19];
-    F[0] = from_bits(bits[0], s0);
+    if (FIXED) {
+        F[0] = from_bits_fixed<1021u>(bits[0], fbad);
 #pragma unroll
-    for (int j = 1; j < 19; j++) F[j] = from_bits(bits[j], s12);
+        for (int j = 1; j < 19; j++)
+            F[j] = j <= 6 ? from_bits_fixed<1018u>(bits[j], fbad)
+                          : from_bits_fixed<1017u>(bits[j], fbad);
+    } else {
+        F[0] = from_bits(bits[0], s0);
+#pragma unroll
+        for (int j = 1; j < 19; j++) F[j] = from_bits(bits[j], s12);
+    }
 
     /* exact moments: rho and J from pair sums / differences */
     int64_t R = F[0], Jx = 0, Jy = 0, Jz = 0;
@@ -283,7 +318,7 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t qd = -mul(split(JJ15), INVs);
         const int64_t G = W00 + mul(T00, split(qd));
         const int64_t Fn = F[0] - mul(oms, split(F[0] - k.tp[0])) + G;
-        bits[0] = to_bits(Fn, rmax);
+        bits[0] = FIXED ? to_bits_fixed<1021u>(Fn, fbad) : to_bits(Fn, rmax);
     }
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
@@ -312,10 +347,20 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t GK = WK + mul(TK, split(qd - t3));
         const int64_t FnJ = F[J] - mul(oms, split(F[J] - tpc)) + GJ;
         const int64_t FnK = F[K] - mul(oms, split(F[K] - tpc)) + GK;
-        bits[J] = to_bits(FnJ, rmax);
-        bits[K] = to_bits(FnK, rmax);
+        if (FIXED) {
+            if (c == 1) {
+                bits[J] = to_bits_fixed<1018u>(FnJ, fbad);
+                bits[K] = to_bits_fixed<1018u>(FnK, fbad);
+            } else {
+                bits[J] = to_bits_fixed<1017u>(FnJ, fbad);
+                bits[K] = to_bits_fixed<1017u>(FnK, fbad);
+            }
+        } else {
+            bits[J] = to_bits(FnJ, rmax);
+            bits[K] = to_bits(FnK, rmax);
+        }
     }
-    const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u);
+    const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u) | (fbad != 0u);
     return flags | (bad ? kBad : 0u);
 }
 

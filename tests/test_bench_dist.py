@@ -1,0 +1,55 @@
+"""The multi-rank plumbing of bench.py on CPU with gloo (world size 2):
+max-over-ranks timing, and the reference arm printing on rank 0 only."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port),
+                      RANK=str(rank), WORLD_SIZE=str(world))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    got = bench.max_over_ranks(10.0 * (rank + 1), world, device="cpu")
+    r, w, _ = bench.dist_env()
+    dist.destroy_process_group()
+    q.put((rank, got, r, w))
+
+
+def test_max_over_ranks_gloo():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r[1] for r in res] == [20.0, 20.0]
+    assert [(r[2], r[3]) for r in res] == [(0, 2), (1, 2)]
+
+
+def test_reference_arm_silent_off_rank0(monkeypatch, capsys):
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference"])
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    bench.main()
+    assert capsys.readouterr().out == ""
