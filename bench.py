@@ -246,30 +246,41 @@ def run_gpu(args, rank, world, local):
     kd, _ = sim.permeability()
     sim.close()
 
-    # end to end through the C ABI from host buffers: table upload and
-    # device build, init, S steps, macro read-back, every step
+    # End to end through the C ABI from host buffers, every call: the host
+    # flag grid (preprocess's input) goes up, preprocess + alloc run on the
+    # device (plb_create_from_flag), init, S lattice steps, and the macros
+    # come back.  The same through the V.bin table (plb_create from 152-byte
+    # records) is reported beside it.
     e2e_steps = args.e2e_steps
     Vh = np.ascontiguousarray(V)
+    fh = np.ascontiguousarray(flag)
     rho = np.empty((4, N))
-    e2e_vals = []
-    for k in range(args.e2e_reps + 1 if args.e2e_reps > 0 else 0):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s2 = P.Simulation(Vh, *dims, vs, tau=w["tau"], force=w["force"],
-                          precision=prec, device=local)
-        s2.init_dist_macro()
-        s2.step(e2e_steps)
-        rho[:] = s2.macros()
-        s2.close()
-        el = time.perf_counter() - t0
-        if k > 0:
-            e2e_vals.append(N * e2e_steps / el / 1e6)
-    if e2e_vals:
+
+    def e2e_rate(make):
+        vals = []
+        for k in range(args.e2e_reps + 1 if args.e2e_reps > 0 else 0):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s2 = make()
+            s2.init_dist_macro()
+            s2.step(e2e_steps)
+            rho[:] = s2.macros()
+            s2.close()
+            el = time.perf_counter() - t0
+            if k > 0:
+                vals.append(N * e2e_steps / el / 1e6)
+        if not vals:
+            return None
         # whole-job rate: the slowest rank's time for the same per-rank work
-        t_rank = N * e2e_steps / (statistics.median(e2e_vals) * 1e6)
-        e2e = N * e2e_steps * world / max_over_ranks(t_rank, world) / 1e6
-    else:
-        e2e = None
+        t_rank = N * e2e_steps / (statistics.median(vals) * 1e6)
+        return N * e2e_steps * world / max_over_ranks(t_rank, world) / 1e6
+
+    e2e = e2e_rate(lambda: P.Simulation.from_flag(
+        fh, *dims, tau=w["tau"], force=w["force"], precision=prec,
+        device=local))
+    e2e_v = e2e_rate(lambda: P.Simulation(
+        Vh, *dims, vs, tau=w["tau"], force=w["force"], precision=prec,
+        device=local))
 
     peak, peak_kind = hbm_peak()
     bpn = BYTES_PER_NODE[prec]
@@ -293,9 +304,14 @@ def run_gpu(args, rank, world, local):
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "bytes_per_node": bpn, "peak_kind": peak_kind},
         "e2e": {"value": round(e2e, 3) if e2e else None, "unit": "MLUPS",
-                "h2d_bytes_per_step": int(Vh.nbytes),
+                "h2d_bytes_per_step": int(fh.nbytes),
                 "d2h_bytes_per_step": int(rho.nbytes),
-                "lattice_steps_per_call": e2e_steps},
+                "lattice_steps_per_call": e2e_steps,
+                "path": "host flag grid -> plb_create_from_flag -> steps -> macros"},
+        "e2e_vbin": {"value": round(e2e_v, 3) if e2e_v else None,
+                     "unit": "MLUPS", "h2d_bytes_per_step": int(Vh.nbytes),
+                     "d2h_bytes_per_step": int(rho.nbytes),
+                     "path": "host V.bin table -> plb_create -> steps -> macros"},
         "gpu_launches": args.steps,
         "clocks": clk.result,
     }
