@@ -277,6 +277,25 @@ int plb_batch_info(plb_batch *b, long long *t, int *active,
 int plb_batch_sample_nodes(plb_batch *b, int id, int *num_node);
 void *plb_batch_stream(plb_batch *b);
 
+/* ------------------------------------------------------- no allocation */
+
+/* No counterpart in the reference.  Sum of ux[0..n) and of rho[0..n)
+ * (caller's device arrays) into out[0], out[1] (caller's device memory), on
+ * `stream` (a cudaStream_t, NULL = legacy default), without allocating: for
+ * callers that cannot let a library allocate device memory (a framework
+ * that owns all device memory through its own pool and budget, a serving
+ * loop admitting work against a fixed HBM budget, code that must not
+ * synchronise the device the way cudaMalloc/cudaFree can).  Its per-block
+ * partial sums live in one fixed 4 MiB device array that every GPU loading
+ * this library holds until exit, so n is limited to
+ * PLB_REDUCE_NOALLOC_MAX_NODES (larger n: PLB_ERR_ARG, nothing launched).
+ * Calls share that array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture.  Asynchronous: out is valid once the stream reaches it. */
+#define PLB_REDUCE_NOALLOC_MAX_NODES 67108864LL
+int plb_reduce_noalloc(const double *ux, const double *rho, long long n,
+                       double *out, void *stream);
+
 /* Human-readable text for a status code. */
 const char *plb_status_string(int status);
 

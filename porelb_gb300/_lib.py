@@ -30,6 +30,7 @@ ERR_NOMEM, ERR_DENSITY, ERR_NUMP, ERR_STATE = -5, -6, -7, -8
 FP64_EXACT, FP64, FP32, FP16DEV, BF16DEV, FP64_FMA = 0, 1, 2, 3, 4, 5
 ORDER_MORTON, ORDER_REFERENCE = 0, 1
 HALO_AUTO, HALO_SINGLE, HALO_REMOTE_WINS = -1, 0, 1
+REDUCE_NOALLOC_MAX_NODES = 67108864
 BOUNDARY_REFERENCE, BOUNDARY_HALFWAY = 0, 1
 
 
@@ -108,6 +109,7 @@ _SIGS = {
                             ctypes.POINTER(ctypes.c_size_t)]),
     "plb_batch_sample_nodes": (_I, [_P, _I, _IP]),
     "plb_batch_stream": (_P, [_P]),
+    "plb_reduce_noalloc": (_I, [_P, _P, ctypes.c_longlong, _P, _P]),
 }
 
 _lib = None
