@@ -124,7 +124,7 @@ def sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, device=0):
 
 
 def _params(tau, force, precision, ordering, halo, block_size, device,
-            boundary="reference"):
+            boundary="reference", kernel_variant=0):
     lib = _lib.load()
     p = _lib.Params()
     lib.plb_default_params(ctypes.byref(p))
@@ -135,6 +135,7 @@ def _params(tau, force, precision, ordering, halo, block_size, device,
     p.block_size = block_size
     p.device = device
     p.boundary = BOUNDARIES[boundary]
+    p.kernel_variant = kernel_variant
     return p
 
 
@@ -145,7 +146,8 @@ class Simulation:
 
     def __init__(self, V, nx, ny, nz, v_sub_start=None, tau=0.8,
                  force=1e-3, precision="fp64_exact", ordering="morton",
-                 halo="auto", block_size=0, device=0, boundary="reference"):
+                 halo="auto", block_size=0, device=0, boundary="reference",
+                 kernel_variant=0):
         self._lib = _lib.load()
         self.V = np.ascontiguousarray(V, dtype=NODE_DTYPE)
         self.nx, self.ny, self.nz = nx, ny, nz
@@ -155,7 +157,7 @@ class Simulation:
         self.tau, self.force = float(tau), float(force)
         self.precision = precision
         p = _params(tau, force, precision, ordering, halo, block_size, device,
-                    boundary)
+                    boundary, kernel_variant)
         h = ctypes.c_void_p()
         _check(self._lib.plb_create(_ptr(self.V), len(self.V), nx, ny, nz,
                                     self.num_p, _iptr(self.v_sub_start),
@@ -256,14 +258,15 @@ class Simulation:
     @classmethod
     def from_flag(cls, flag, nx, ny, nz, num_p=1, tau=0.8, force=1e-3,
                   precision="fp64_exact", ordering="morton", halo="auto",
-                  block_size=0, device=0, boundary="reference"):
+                  block_size=0, device=0, boundary="reference",
+                  kernel_variant=0):
         """build_V + create on the device from a 0/1 flag grid."""
         lib = _lib.load()
         flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
         if flag.size != nx * ny * nz:
             raise ValueError("flag size does not match nx*ny*nz")
         p = _params(tau, force, precision, ordering, halo, block_size, device,
-                    boundary)
+                    boundary, kernel_variant)
         h = ctypes.c_void_p()
         _check(lib.plb_create_from_flag(_ptr(flag), nx, ny, nz, num_p,
                                         ctypes.byref(p), ctypes.byref(h)),

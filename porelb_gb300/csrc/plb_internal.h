@@ -115,7 +115,7 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
 
 /* Launch one step of the given precision. */
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
-                        int block, cudaStream_t s);
+                        int block, int variant, cudaStream_t s);
 
 /* One step of every active block of a batch pool (256 nodes per block). */
 constexpr int kBatchBlock = 256;

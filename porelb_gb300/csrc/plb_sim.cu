@@ -26,7 +26,7 @@ extern "C" void plb_host_constants(double tau, double force, double *omega,
 struct plb_sim {
     int n, nx, ny, nz, num_p;
     long long npad;
-    int precision, ordering, halo, block, boundary;
+    int precision, ordering, halo, block, boundary, variant;
     int device;
     cudaStream_t stream;
     void *f[2];
@@ -647,7 +647,11 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->ordering = p->ordering;
     s->halo = p->halo;
     s->boundary = p->boundary;
-    s->block = p->block_size > 0 ? p->block_size : 256;
+    /* the 80-register FP64 kernel is the faster one on GB300 (launch tuner:
+     * 12.6 vs 11.8 GLUPS at 256^3); kernel_variant 2 asks for the other */
+    s->variant = p->precision == PLB_FP64 ? (p->kernel_variant == 2 ? 0 : 1) : 0;
+    s->block = p->block_size > 0 ? p->block_size
+                                 : (p->precision == PLB_FP64 ? 128 : 256);
     if (s->block > 256 || (s->block & 31)) s->block = 256;
     s->device = p->device;
     s->elem = elem_size(p->precision);
@@ -904,7 +908,7 @@ int plb_step_async(plb_sim *s, int it_begin, int nsteps)
         a.fout = s->f[s->cur ^ 1];
         a.co.it = it_begin + k;
         const bool last = (k == nsteps - 1);
-        cudaError_t e = launch_step(s->precision, last, a, s->block, s->stream);
+        cudaError_t e = launch_step(s->precision, last, a, s->block, s->variant, s->stream);
         if (e != cudaSuccess) {
             fprintf(stderr, "porelb_gpu: step launch failed: %s\n", cudaGetErrorString(e));
             return PLB_ERR_CUDA;

@@ -328,9 +328,12 @@ template <> struct StoreOf<PLB_FP32> { using T = float; };
 template <> struct StoreOf<PLB_FP16DEV> { using T = __half; };
 template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
 
-/* resident blocks of 256 threads per SM the register budget is set for */
-template <int PREC> struct MinBlocks { static constexpr int v = 1; };
-template <> struct MinBlocks<PLB_FP64> { static constexpr int v = 2; };
+/* resident blocks of 256 threads per SM the register budget is set for;
+ * the FP64 form has a second variant with a tighter budget (80 registers,
+ * 24 warps per SM) for the launch tuner */
+template <int PREC, int V> struct MinBlocks { static constexpr int v = 1; };
+template <> struct MinBlocks<PLB_FP64, 0> { static constexpr int v = 2; };
+template <> struct MinBlocks<PLB_FP64, 1> { static constexpr int v = 3; };
 
 /* Gather, collide and store node i.  Returns the macros; *dev_max receives
  * the largest stored deviation magnitude of the 16-bit forms. */
@@ -381,8 +384,8 @@ __device__ __forceinline__ Macro step_node(const void *fin_, void *fout_,
     return m;
 }
 
-template <int PREC, bool MACRO>
-__global__ void __launch_bounds__(256, MinBlocks<PREC>::v)
+template <int PREC, bool MACRO, int VARIANT>
+__global__ void __launch_bounds__(256, MinBlocks<PREC, VARIANT>::v)
 k_step(const StepArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -429,7 +432,7 @@ k_step(const StepArgs a)
 
 /* Batch step: block b belongs to sample blk_sample[b] (or is free). */
 template <int PREC, bool MACRO>
-__global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC>::v)
+__global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC, 1>::v)
 k_batch_step(const BatchArgs a)
 {
     const int s = a.blk_sample[blockIdx.x];
@@ -487,12 +490,17 @@ k_batch_step(const BatchArgs a)
 
 template <int PREC>
 static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
-                               cudaStream_t s)
+                               int variant, cudaStream_t s)
 {
     const int grid = (a.n + block - 1) / block;
     if (grid == 0) return cudaSuccess;
-    if (macros) k_step<PREC, true><<<grid, block, 0, s>>>(a);
-    else k_step<PREC, false><<<grid, block, 0, s>>>(a);
+    if (PREC == PLB_FP64 && variant == 1) {
+        if (macros) k_step<PREC, true, 1><<<grid, block, 0, s>>>(a);
+        else k_step<PREC, false, 1><<<grid, block, 0, s>>>(a);
+    } else {
+        if (macros) k_step<PREC, true, 0><<<grid, block, 0, s>>>(a);
+        else k_step<PREC, false, 0><<<grid, block, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
@@ -521,15 +529,15 @@ cudaError_t launch_batch_step(int precision, bool macros, const BatchArgs &a,
 }
 
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
-                        int block, cudaStream_t s)
+                        int block, int variant, cudaStream_t s)
 {
     switch (precision) {
-    case PLB_FP64_EXACT: return launch_prec<PLB_FP64_EXACT>(macros, a, block, s);
-    case PLB_FP64: return launch_prec<PLB_FP64>(macros, a, block, s);
-    case PLB_FP64_FMA: return launch_prec<PLB_FP64_FMA>(macros, a, block, s);
-    case PLB_FP32: return launch_prec<PLB_FP32>(macros, a, block, s);
-    case PLB_FP16DEV: return launch_prec<PLB_FP16DEV>(macros, a, block, s);
-    case PLB_BF16DEV: return launch_prec<PLB_BF16DEV>(macros, a, block, s);
+    case PLB_FP64_EXACT: return launch_prec<PLB_FP64_EXACT>(macros, a, block, variant, s);
+    case PLB_FP64: return launch_prec<PLB_FP64>(macros, a, block, variant, s);
+    case PLB_FP64_FMA: return launch_prec<PLB_FP64_FMA>(macros, a, block, variant, s);
+    case PLB_FP32: return launch_prec<PLB_FP32>(macros, a, block, variant, s);
+    case PLB_FP16DEV: return launch_prec<PLB_FP16DEV>(macros, a, block, variant, s);
+    case PLB_BF16DEV: return launch_prec<PLB_BF16DEV>(macros, a, block, variant, s);
     default: return cudaErrorInvalidValue;
     }
 }

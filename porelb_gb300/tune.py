@@ -1,10 +1,12 @@
-"""Autotuner for the step launch: threads per block and node ordering.
+"""Autotuner for the step launch: threads per block, register budget and
+node ordering.
 
 For one geometry and storage form it builds a solver per candidate
-(block size in {64, 128, 256}, Morton or reference node order), times a few
-steps with CUDA events on the solver's stream after a warm-up, and keeps the
-fastest.  Results are cached per (form, boundary, node-count bucket) for the
-process; ``best`` returns the cached choice when one exists.
+(block size in {64, 128, 256}; for FP64 the 128- and 80-register kernels;
+Morton or reference node order), times a few steps with CUDA events on the
+solver's stream after a warm-up, and keeps the fastest.  Results are cached
+per (form, boundary, node-count bucket) for the process; ``best`` returns the
+cached choice when one exists.
 """
 import math
 
@@ -20,12 +22,13 @@ def _bucket(n):
 
 
 def time_config(flag, dims, precision, block, ordering, tau=0.8, force=1e-5,
-                steps=20, warmup=5, boundary="reference"):
+                steps=20, warmup=5, boundary="reference", variant=0):
     """Mean milliseconds per step of one configuration."""
     import torch
     sim = Simulation.from_flag(flag, *dims, tau=tau, force=force,
                                precision=precision, ordering=ordering,
-                               block_size=block, boundary=boundary)
+                               block_size=block, boundary=boundary,
+                               kernel_variant=variant)
     try:
         sim.init_dist_macro()
         sim.step(warmup)
@@ -42,21 +45,23 @@ def time_config(flag, dims, precision, block, ordering, tau=0.8, force=1e-5,
 
 
 def tune(flag, dims, precision="fp64", boundary="reference", steps=20):
-    """Time every candidate; returns (best, table of (block, ordering, ms))."""
+    """Time every candidate; returns (best, [(block, ordering, variant, ms)])."""
     table = []
     n = None
+    variants = (1, 2) if precision == "fp64" else (0,)
     for ordering in ORDERINGS:
         for block in BLOCKS:
-            ms, n = time_config(flag, dims, precision, block, ordering,
-                                steps=steps, boundary=boundary)
-            table.append((block, ordering, ms))
-    best = min(table, key=lambda r: r[2])
-    _cache[(precision, boundary, _bucket(n))] = dict(block_size=best[0],
-                                                    ordering=best[1])
-    return dict(block_size=best[0], ordering=best[1], ms=best[2]), table
+            for v in variants:
+                ms, n = time_config(flag, dims, precision, block, ordering,
+                                    steps=steps, boundary=boundary, variant=v)
+                table.append((block, ordering, v, ms))
+    best = min(table, key=lambda r: r[3])
+    choice = dict(block_size=best[0], ordering=best[1], kernel_variant=best[2])
+    _cache[(precision, boundary, _bucket(n))] = choice
+    return dict(choice, ms=best[3]), table
 
 
 def best(precision, n, boundary="reference"):
     """Cached choice for this form and size, or the defaults."""
     return _cache.get((precision, boundary, _bucket(n)),
-                      dict(block_size=256, ordering="morton"))
+                      dict(block_size=0, ordering="morton", kernel_variant=0))

@@ -250,3 +250,27 @@ def test_fp64_fixed_point_matches_cpu_twin_bitwise(tmp_path):
     with gpu_run(V, dims, vs, 0.7, 2e-4, 60, precision="fp64") as sim:
         assert (sim.get_f() == f0).all()
         assert (sim.macros()[0] == mac[0]).all()
+
+
+def test_dropin_porelb_x_dumps_match_reference(tmp_path):
+    """preprocess.x + porelb.x on the 64^3 configuration write the
+    reference's part files byte for byte (FP64_EXACT form)."""
+    import subprocess
+    bin_dir = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "porelb_gb300", "bin")
+    m = META["c1_64_seed0"]
+    geo = m["geometry"]
+    flag = pack_flag(m["dims"], geo["seed"], geo["rmin"], geo["rmax"],
+                     geo["porosity"])
+    flag.tofile(tmp_path / "flag.bin")
+    subprocess.run([os.path.join(bin_dir, "preprocess.x"), "1",
+                    *map(str, m["dims"])], cwd=tmp_path, check=True,
+                   capture_output=True)
+    r = subprocess.run([os.path.join(bin_dir, "porelb.x"), "1000", "--tau",
+                        repr(m["tau"]), "--force", repr(m["force"]),
+                        "--precision", "fp64_exact"], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for fn, h in m["parts"].items():
+        with open(tmp_path / fn, "rb") as fh:
+            assert hashlib.sha256(fh.read()).hexdigest() == h, fn
