@@ -106,7 +106,8 @@ typedef struct {
     int boundary;    /* PLB_BOUNDARY_REFERENCE (default) or PLB_BOUNDARY_HALFWAY */
     int kernel_variant; /* PLB_FP64 only: 0 or 1 = 80-register step kernel
                            (24 warps per SM, the default), 2 = 128-register
-                           kernel (16 warps per SM) */
+                           kernel (16 warps per SM), 3 = 64-register kernel
+                           (32 warps per SM) */
     int reserved[5];
 } plb_params;
 

@@ -18,10 +18,10 @@
  *
  *   f'_j = f_j - w (f_j - w_j) + G_j
  *   G_j  = w_j [ w delta + c (e_jx rho - J_x)
- *                + (w + c e_jx - c u_x) (3 e_j.J + (4.5 (e_j.J)^2 - 1.5 J.J)/rho) ]
+ *                + (w + c e_jx - c u_x) (3 e_j.J + 4.5 (e_j.J)(e_j.u) - 1.5 J.u) ]
  *
- * with c = 3 (1 - w/2) F and w_j the lattice weights.  Every term is exact
- * algebra of the reference's expression.
+ * with c = 3 (1 - w/2) F, u = J/rho and w_j the lattice weights.  Every
+ * term is exact algebra of the reference's expression.
  *
  * Range: collide<false> requires f_0 in [2^-8, 1) and f_j in [2^-8, 1/4)
  * for j > 0, rho in [0.5, 1.2], and results in [2^-8, 8); collide<true>
@@ -293,11 +293,14 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
     mom.Jz = Jz;
     mom.inv = INV;
 
+    /* u = J / rho; then (e.J)^2 / rho = (e.J)(e.u) and J.J / rho = J.u, so
+     * the quadratic terms need one product per direction pair */
     const Sp Jxs = split(Jx), Jys = split(Jy), Jzs = split(Jz);
-    const int64_t JJ = mul(Jxs, Jxs) + mul(Jys, Jys) + mul(Jzs, Jzs);
-    const int64_t JJ15 = JJ + (JJ >> 1);
+    const int64_t ux = mul(Jxs, INVs), uy = mul(Jys, INVs), uz = mul(Jzs, INVs);
+    const int64_t Ju = mul(Jxs, split(ux)) + mul(Jys, split(uy)) + mul(Jzs, split(uz));
+    const int64_t Ju15 = Ju + (Ju >> 1);
     const Sp oms = split(k.om), cfs = split(k.cf);
-    const int64_t cux = mul(cfs, split(mul(Jxs, INVs)));
+    const int64_t cux = mul(cfs, split(ux));
     const int64_t A0 = k.om - cux, Ap = A0 + k.cf, Am = A0 - k.cf;
     const int64_t cJx = mul(cfs, Jxs), cR = mul(cfs, Rs);
     const int64_t B0 = mul(oms, split(R - kOne)) - cJx, Bp = B0 + cR, Bm = B0 - cR;
@@ -315,7 +318,7 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
 
     /* rest direction: e.J = 0 */
     {
-        const int64_t qd = -mul(split(JJ15), INVs);
+        const int64_t qd = -Ju15;
         const int64_t G = W00 + mul(T00, split(qd));
         const int64_t Fn = F[0] - mul(oms, split(F[0] - k.tp[0])) + G;
         bits[0] = FIXED ? to_bits_fixed<1021u>(Fn, fbad) : to_bits(Fn, rmax);
@@ -323,14 +326,12 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
         const int K = J + 1;
-        int64_t ej = 0;
-        if (fex(J) > 0) ej += Jx; else if (fex(J) < 0) ej -= Jx;
-        if (fey(J) > 0) ej += Jy; else if (fey(J) < 0) ej -= Jy;
-        if (fez(J) > 0) ej += Jz; else if (fez(J) < 0) ej -= Jz;
-        const Sp ejs = split(ej);
-        const int64_t ej2 = mul(ejs, ejs);
-        const int64_t q = ej2 * 4 + (ej2 >> 1) - JJ15;
-        const int64_t qd = mul(split(q), INVs);
+        int64_t ej = 0, eu = 0;
+        if (fex(J) > 0) { ej += Jx; eu += ux; } else if (fex(J) < 0) { ej -= Jx; eu -= ux; }
+        if (fey(J) > 0) { ej += Jy; eu += uy; } else if (fey(J) < 0) { ej -= Jy; eu -= uy; }
+        if (fez(J) > 0) { ej += Jz; eu += uz; } else if (fez(J) < 0) { ej -= Jz; eu -= uz; }
+        const int64_t e2 = mul(split(ej), split(eu)); /* (e.J)^2 / rho */
+        const int64_t qd = e2 * 4 + (e2 >> 1) - Ju15; /* (4.5 (e.J)^2 - 1.5 J.J)/rho */
         const int64_t t3 = ej * 3;
         const int c = fcls(J);
         const int64_t tpc = c == 1 ? k.tp[1] : k.tp[2];

@@ -649,7 +649,9 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->boundary = p->boundary;
     /* the 80-register FP64 kernel is the faster one on GB300 (launch tuner:
      * 12.6 vs 11.8 GLUPS at 256^3); kernel_variant 2 asks for the other */
-    s->variant = p->precision == PLB_FP64 ? (p->kernel_variant == 2 ? 0 : 1) : 0;
+    s->variant = p->precision == PLB_FP64
+                     ? (p->kernel_variant == 2 ? 0 : (p->kernel_variant == 3 ? 3 : 1))
+                     : 0;
     s->block = p->block_size > 0 ? p->block_size
                                  : (p->precision == PLB_FP64 ? 128 : 256);
     if (s->block > 256 || (s->block & 31)) s->block = 256;

@@ -334,6 +334,7 @@ template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
 template <int PREC, int V> struct MinBlocks { static constexpr int v = 1; };
 template <> struct MinBlocks<PLB_FP64, 0> { static constexpr int v = 2; };
 template <> struct MinBlocks<PLB_FP64, 1> { static constexpr int v = 3; };
+template <> struct MinBlocks<PLB_FP64, 3> { static constexpr int v = 4; };
 
 /* Gather, collide and store node i.  Returns the macros; *dev_max receives
  * the largest stored deviation magnitude of the 16-bit forms. */
@@ -438,8 +439,17 @@ k_batch_step(const BatchArgs a)
     const int s = a.blk_sample[blockIdx.x];
     double sum_u = 0.0, sum_r = 0.0;
     float dmax = 0.f;
+    /* the block's sample record, staged once in shared memory */
+    __shared__ SampleDev sp;
     if (s >= 0) {
-        const SampleDev &sp = a.samples[s];
+        constexpr int words = (int)(sizeof(SampleDev) / 4);
+        static_assert(sizeof(SampleDev) % 4 == 0, "SampleDev is copied as words");
+        const uint32_t *src = (const uint32_t *)(a.samples + s);
+        uint32_t *dst = (uint32_t *)&sp;
+        for (int k = threadIdx.x; k < words; k += kBatchBlock) dst[k] = src[k];
+    }
+    __syncthreads();
+    if (s >= 0) {
         const long long i = (long long)blockIdx.x * kBatchBlock + threadIdx.x;
         if (i - sp.base < sp.n) {
             Coeffs co = sp.co;
@@ -497,6 +507,9 @@ static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
     if (PREC == PLB_FP64 && variant == 1) {
         if (macros) k_step<PREC, true, 1><<<grid, block, 0, s>>>(a);
         else k_step<PREC, false, 1><<<grid, block, 0, s>>>(a);
+    } else if (PREC == PLB_FP64 && variant == 3) {
+        if (macros) k_step<PREC, true, 3><<<grid, block, 0, s>>>(a);
+        else k_step<PREC, false, 3><<<grid, block, 0, s>>>(a);
     } else {
         if (macros) k_step<PREC, true, 0><<<grid, block, 0, s>>>(a);
         else k_step<PREC, false, 0><<<grid, block, 0, s>>>(a);
