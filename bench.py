@@ -439,6 +439,9 @@ def run_served(args):
                               "max": max(errs) if errs else None,
                               "median": statistics.median(errs) if errs else None},
         "fp64_mlups_on_checked": round(ns64 / wall64 / 1e6, 1) if wall64 else None,
+        "time_split_s": {"admission": round(summ["admit_s"], 2),
+                         "batch_run": round(summ["run_s"], 2),
+                         "wall": round(summ["wall_s"], 2)},
         "config": {"workload": f"{len(reqs)} Poisson requests, seed 4",
                    "rate_per_s": args.rate, "budget_gb": args.budget_gb,
                    "check_every": args.check_every,

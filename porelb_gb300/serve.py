@@ -43,6 +43,7 @@ class Server:
         t0 = time.perf_counter()
         node_steps = 0
         intervals = 0
+        t_admit = t_run = 0.0
         K = self.batch.check_every
         while pending or waiting or live:
             now = time.perf_counter() - t0
@@ -53,6 +54,7 @@ class Server:
             # admission: FCFS with bounded lookahead past a head that does
             # not fit into the free node ranges
             admitted = []
+            ta = time.perf_counter()
             for r in waiting[: self.lookahead]:
                 sid = self.batch.try_add_packed(
                     r.seed, r.edge, r.edge, r.edge, r.rmin, r.rmax, r.porosity,
@@ -63,13 +65,16 @@ class Server:
                     admitted.append(r)
             for r in admitted:
                 waiting.remove(r)
+            t_admit += time.perf_counter() - ta
             if not live:
                 if pending:
                     time.sleep(max(0.0, pending[0].arrival * time_scale -
                                    (time.perf_counter() - t0)))
                 continue
             node_steps += sum(v["nodes"] for v in live.values()) * K
+            tr = time.perf_counter()
             self.batch.run(1)
+            t_run += time.perf_counter() - tr
             intervals += 1
             for sid in self.batch.poll():
                 res = self.batch.result(sid)
@@ -91,5 +96,6 @@ class Server:
                        p99_latency_s=float(np.percentile(lat, 99)),
                        fluid_mlups=node_steps / wall / 1e6 if wall > 0 else 0.0,
                        intervals=intervals, capacity_nodes=self.capacity,
+                       admit_s=t_admit, run_s=t_run,
                        precision=self.precision, check_every=K)
         return done, summary
