@@ -412,13 +412,57 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def _plain_fp64_fcfs(reqs, K, max_steps):
+    """The FP64 plain form serving the same requests one at a time, first
+    come first served: each request is solved alone (FP64 fixed-point step,
+    same steady-state test every K steps); queueing is replayed on the
+    arrival times with the measured solve times."""
+    import torch
+    import porelb_gb300 as P
+    ks, service = {}, []
+    for r in reqs:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim = P.Simulation.packed(r.seed, r.edge, r.edge, r.edge, r.rmin,
+                                  r.rmax, r.porosity, tau=r.tau, force=r.force,
+                                  precision="fp64")
+        sim.init_dist_macro()
+        it, prev, k, checks = 0, None, None, 0
+        while it < max_steps:
+            sim.step(K, it_begin=it)
+            it += K
+            k = sim.permeability()[0]
+            checks += 1
+            if checks >= 2 and k != 0 and abs(k - prev) <= r.tol * abs(k):
+                break
+            prev = k
+        sim.close()
+        service.append(time.perf_counter() - t0)
+        ks[r.index] = k
+    t_free, lat = 0.0, []
+    for r, sv in zip(reqs, service):
+        start = max(r.arrival, t_free)
+        t_free = start + sv
+        lat.append(t_free - r.arrival)
+    span = t_free - reqs[0].arrival
+    return ks, dict(solves_per_s=len(reqs) / span if span > 0 else None,
+                    p50_latency_s=float(np.percentile(lat, 50)),
+                    p99_latency_s=float(np.percentile(lat, 99)),
+                    mean_solve_s=float(np.mean(service)))
+
+
+SERVE_FORMS = {"fp16dev": "FP16 deviations", "bf16dev": "BF16 deviations",
+               "fp32": "FP32", "fp64": "FP64"}
+
+
 def run_served(args):
     import torch
     from porelb_gb300.serve import Server
     from porelb_gb300.workloads import serving_requests
     torch.cuda.set_device(0)
     reqs = serving_requests(args.requests, 4, args.rate)
-    srv = Server(args.budget_gb * 1e9, "fp16dev", check_every=args.check_every)
+    srv = Server(args.budget_gb * 1e9, args.serve_precision,
+                 check_every=args.check_every)
     done, summ = srv.serve(reqs, max_wall=args.max_wall)
     srv.close()
     # FP64 plain form on a sample of the same requests, one at a time
@@ -428,8 +472,17 @@ def run_served(args):
     by = {d["index"]: d for d in done}
     errs = [abs(by[i]["k_darcy"] - r["k_darcy"]) / abs(r["k_darcy"])
             for i, r in res64.items() if r["k_darcy"]]
+    plain = None
+    if args.plain_fp64:
+        served = [r for r in reqs if r.index in by]
+        ks64, plain = _plain_fp64_fcfs(served, args.check_every, args.max_steps)
+        perr = [abs(by[i]["k_darcy"] - k) / abs(k) for i, k in ks64.items() if k]
+        plain["k_rel_err_served_vs_plain_fp64"] = {
+            "max": max(perr) if perr else None,
+            "median": statistics.median(perr) if perr else None,
+            "within_1e-3": sum(e <= 1e-3 for e in perr), "of": len(perr)}
     line = {
-        "metric": "perm solves/s (served, FP16 deviations)",
+        "metric": "perm solves/s (served, %s)" % SERVE_FORMS[args.serve_precision],
         "value": round(summ["solves_per_s"], 3), "unit": "solves/s",
         "p50_latency_s": round(summ["p50_latency_s"], 3),
         "p99_latency_s": round(summ["p99_latency_s"], 3),
@@ -439,6 +492,7 @@ def run_served(args):
                               "max": max(errs) if errs else None,
                               "median": statistics.median(errs) if errs else None},
         "fp64_mlups_on_checked": round(ns64 / wall64 / 1e6, 1) if wall64 else None,
+        "plain_fp64_fcfs": plain,
         "time_split_s": {"admission": round(summ["admit_s"], 2),
                          "batch_run": round(summ["run_s"], 2),
                          "wall": round(summ["wall_s"], 2)},
@@ -517,6 +571,11 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=80.0)
     ap.add_argument("--max-wall", type=float, default=None)
     ap.add_argument("--fp64-check", type=int, default=32)
+    ap.add_argument("--serve-precision", default="fp16dev",
+                    choices=sorted(SERVE_FORMS))
+    ap.add_argument("--plain-fp64", action="store_true",
+                    help="also serve the same requests with the FP64 plain "
+                         "form, one at a time (first come first served)")
     ap.add_argument("--edge", type=int, default=1024)
     args = ap.parse_args()
     if args.mode == "batched":

@@ -26,6 +26,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <map>
 #include <type_traits>
 #include <vector>
@@ -211,13 +212,16 @@ struct plb_batch {
     int *t_dev = nullptr;
     double *h_ssum = nullptr;   /* pinned */
     unsigned *h_serr = nullptr; /* pinned */
-    long long t = 0, hw = 0;
+    long long t = 0;
+    int *blist = nullptr;          /* device: active pool blocks */
+    std::vector<int> hlist;        /* host copy */
+    bool list_dirty = true;
     std::map<long long, long long> free_blocks; /* start -> length */
     std::vector<SampleHost> s;
     std::vector<int> done;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    long long graph_hw = -1;
+    long long graph_n = -1;
     int graph_cur = -1;
     size_t bytes = 0;
 };
@@ -252,6 +256,7 @@ static void batch_free(plb_batch *b)
     cudaFree(b->coord);
     cudaFree(b->macro);
     cudaFree(b->blk);
+    cudaFree(b->blist);
     cudaFree(b->sdev);
     cudaFree(b->sactive);
     cudaFree(b->partial);
@@ -310,6 +315,7 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
     al(&b->coord, 2 * 3 * np);
     if (keep_macros) al(&b->macro, 8 * 4 * np);
     al(&b->blk, 4 * (size_t)b->cap_blocks);
+    al(&b->blist, 4 * (size_t)b->cap_blocks);
     al(&b->sdev, sizeof(SampleDev) * (size_t)max_samples);
     al(&b->sactive, 4 * (size_t)max_samples);
     al(&b->partial, 8 * 3 * (size_t)b->cap_blocks);
@@ -441,7 +447,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     k_set_blocks<<<gb(nblk, B), B, 0, b->st>>>(b->blk, blk0, nblk, sid);
     BCK(cudaGetLastError());
     BCK(cudaStreamSynchronize(b->st));
-    if (blk0 + nblk > b->hw) b->hw = blk0 + nblk;
+    b->list_dirty = true;
     *id = sid;
     return PLB_OK;
 }
@@ -498,12 +504,14 @@ static int build_graph(plb_batch *b)
         cudaGraphDestroy(b->graph);
         b->graph = nullptr;
     }
-    const int nb = (int)b->hw;
+    const int nb = (int)b->hlist.size();
     BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     BatchArgs a;
     memset(&a, 0, sizeof(a));
     a.nbr = b->nbr;
     a.npad = b->npad;
+    a.blk_list = b->blist;
+    a.part_stride = b->cap_blocks;
     a.blk_sample = b->blk;
     a.samples = b->sdev;
     a.t_base = b->t_dev;
@@ -521,8 +529,8 @@ static int build_graph(plb_batch *b)
     }
     if (e == cudaSuccess) {
         k_advance<<<1, 1, 0, b->st>>>(b->t_dev, b->K);
-        k_sample_sums<<<b->max_samples, 128, 0, b->st>>>(b->sdev, b->sactive, b->partial, nb,
-                                                         b->ssum);
+        k_sample_sums<<<b->max_samples, 128, 0, b->st>>>(b->sdev, b->sactive, b->partial,
+                                                         (int)b->cap_blocks, b->ssum);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -538,7 +546,7 @@ static int build_graph(plb_batch *b)
         fprintf(stderr, "porelb_gpu: batch graph capture failed: %s\n", cudaGetErrorString(e));
         return PLB_ERR_CUDA;
     }
-    b->graph_hw = b->hw;
+    b->graph_n = nb;
     b->graph_cur = b->cur;
     return PLB_OK;
 }
@@ -553,6 +561,7 @@ static void retire(plb_batch *b, int sid, int status)
     cudaMemcpyAsync(b->sactive + sid, &zero, 4, cudaMemcpyHostToDevice, b->st);
     k_set_blocks<<<gb(h.nblk, B), B, 0, b->st>>>(b->blk, h.blk0, h.nblk, -1);
     free_range(b, h.blk0, h.nblk);
+    b->list_dirty = true;
     b->done.push_back(sid);
 }
 
@@ -564,7 +573,23 @@ int plb_batch_run(plb_batch *b, int intervals, int *n_active)
         int act = 0;
         for (auto &h : b->s) act += h.active;
         if (act == 0) break;
-        if (!b->gexec || b->graph_hw != b->hw || b->graph_cur != b->cur) {
+        if (b->list_dirty) {
+            /* the pool blocks of the active samples, in pool order */
+            std::vector<std::pair<long long, int>> order;
+            for (int sid = 0; sid < b->max_samples; sid++)
+                if (b->s[sid].active) order.emplace_back(b->s[sid].blk0, sid);
+            std::sort(order.begin(), order.end());
+            b->hlist.clear();
+            for (auto &o : order) {
+                const SampleHost &h = b->s[o.second];
+                for (long long k = 0; k < h.nblk; k++) b->hlist.push_back((int)(h.blk0 + k));
+            }
+            if (!b->hlist.empty())
+                BCK(cudaMemcpyAsync(b->blist, b->hlist.data(), 4 * b->hlist.size(),
+                                    cudaMemcpyHostToDevice, b->st));
+            b->list_dirty = false;
+        }
+        if (!b->gexec || b->graph_n != (long long)b->hlist.size() || b->graph_cur != b->cur) {
             int rc = build_graph(b);
             if (rc != PLB_OK) return rc;
         }

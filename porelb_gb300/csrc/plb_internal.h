@@ -88,12 +88,15 @@ struct BatchArgs {
     void *fout;
     const uint32_t *nbr;
     long long npad;
-    const int *blk_sample;     /* sample of every 256-node block, -1 = free */
+    const int *blk_list;       /* pool blocks this launch covers (one CTA each) */
+    const int *blk_sample;     /* sample of every 256-node pool block, -1 = free */
+    long long part_stride;     /* pool blocks: stride of the partial-sum rows */
     const SampleDev *samples;
     const int *t_base;         /* batch step counter (device) */
     int t_off;                 /* this launch's step = *t_base + t_off */
     double *macro;             /* may be NULL */
-    double *partial;           /* [3][gridDim.x]: sum ux, sum rho, max |dev| */
+    double *partial;           /* [3][part_stride] by pool block: sum ux, sum rho,
+                                  max |stored deviation| */
     unsigned int *serr;        /* per-sample error bits */
 };
 

@@ -431,12 +431,14 @@ k_step(const StepArgs a)
     }
 }
 
-/* Batch step: block b belongs to sample blk_sample[b] (or is free). */
+/* Batch step: CTA b works on pool block blk_list[b], which belongs to sample
+ * blk_sample[pool block]. */
 template <int PREC, bool MACRO>
 __global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC, 1>::v)
 k_batch_step(const BatchArgs a)
 {
-    const int s = a.blk_sample[blockIdx.x];
+    const int pb = a.blk_list[blockIdx.x];
+    const int s = a.blk_sample[pb];
     double sum_u = 0.0, sum_r = 0.0;
     float dmax = 0.f;
     /* the block's sample record, staged once in shared memory */
@@ -450,7 +452,7 @@ k_batch_step(const BatchArgs a)
     }
     __syncthreads();
     if (s >= 0) {
-        const long long i = (long long)blockIdx.x * kBatchBlock + threadIdx.x;
+        const long long i = (long long)pb * kBatchBlock + threadIdx.x;
         if (i - sp.base < sp.n) {
             Coeffs co = sp.co;
             co.it = *a.t_base + a.t_off - sp.start;
@@ -491,9 +493,9 @@ k_batch_step(const BatchArgs a)
                 tr += sr[k];
                 td = fmaxf(td, sd[k]);
             }
-            a.partial[blockIdx.x] = tu;
-            a.partial[gridDim.x + blockIdx.x] = tr;
-            a.partial[2 * gridDim.x + blockIdx.x] = (double)td;
+            a.partial[pb] = tu;
+            a.partial[a.part_stride + pb] = tr;
+            a.partial[2 * a.part_stride + pb] = (double)td;
         }
     }
 }
