@@ -223,8 +223,9 @@ def run_gpu(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
+    kv = args.kernel_variant
     sim = P.Simulation(V, *dims, vs, tau=w["tau"], force=w["force"],
-                       precision=prec, device=local)
+                       precision=prec, device=local, kernel_variant=kv)
     sim.init_dist_macro()
     stream = torch.cuda.ExternalStream(sim.stream, device=local)
     it = 0
@@ -277,10 +278,10 @@ def run_gpu(args, rank, world, local):
 
     e2e = e2e_rate(lambda: P.Simulation.from_flag(
         fh, *dims, tau=w["tau"], force=w["force"], precision=prec,
-        device=local))
+        device=local, kernel_variant=kv))
     e2e_v = e2e_rate(lambda: P.Simulation(
         Vh, *dims, vs, tau=w["tau"], force=w["force"], precision=prec,
-        device=local))
+        device=local, kernel_variant=kv))
 
     peak, peak_kind = hbm_peak()
     bpn = BYTES_PER_NODE[prec]
@@ -556,6 +557,8 @@ def main():
     ap.add_argument("--workload", default="c2_256", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="fp64",
                     choices=sorted(BYTES_PER_NODE))
+    ap.add_argument("--kernel-variant", type=int, default=0,
+                    help="FP64 step kernel (0 = the library default)")
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--e2e-reps", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=10.0)

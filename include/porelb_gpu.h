@@ -104,9 +104,9 @@ typedef struct {
     int block_size;  /* threads per block for the step kernel; 0 = default */
     int device;      /* CUDA device ordinal */
     int boundary;    /* PLB_BOUNDARY_REFERENCE (default) or PLB_BOUNDARY_HALFWAY */
-    int kernel_variant; /* PLB_FP64 only: 0 or 1 = 80-register step kernel
-                           (24 warps per SM, the default), 2 = 128-register
-                           kernel (16 warps per SM), 3 = 64-register kernel
+    int kernel_variant; /* PLB_FP64 only: 0 or 2 = 128-register step kernel
+                           (16 warps per SM, the default), 1 = 80-register
+                           kernel (24 warps per SM), 3 = 64-register kernel
                            (32 warps per SM) */
     int reserved[5];
 } plb_params;

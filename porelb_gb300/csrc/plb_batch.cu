@@ -284,7 +284,7 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
     if (!out) return PLB_ERR_ARG;
     *out = nullptr;
     if (capacity_nodes == 0 || max_samples <= 0 || elem_of(precision) == 0 ||
-        check_every <= 0 || (check_every & 1) || capacity_nodes >= (size_t)kSrcMask - B)
+        check_every <= 0 || (check_every & 1) || capacity_nodes >= (size_t)kMaxNodes - B)
         return PLB_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)

@@ -150,12 +150,15 @@ FX_HD uint64_t to_bits(int64_t F, uint32_t &rmax_seen)
 
 /* Fixed-binade forms: the value's biased FP64 exponent is E, the exponent
  * of its lattice weight (1/3 -> 1021, 1/18 -> 1018, 1/36 -> 1017), so every
- * shift is a constant.  A value outside that binade (input or result) sets
- * *bad and the whole node is recomputed by the caller. */
+ * shift is a constant.  A value outside that binade (input or result) sets a
+ * bit at or above bit 20 of *bad (sign and exponent field XOR their expected
+ * value; one three-input logic operation per value) and the whole node is
+ * recomputed by the caller; bits 0..19 of *bad carry mantissa bits and mean
+ * nothing. */
 template <uint32_t E>
 FX_HD int64_t from_bits_fixed(uint64_t b, uint32_t &bad)
 {
-    bad |= (uint32_t)((uint32_t)(b >> 52) != E); /* also catches the sign bit */
+    bad |= (uint32_t)(b >> 32) ^ (E << 20);
     const uint64_t m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
     return (int64_t)(m << (E - 1015u));
 }
@@ -165,8 +168,8 @@ FX_HD uint64_t to_bits_fixed(int64_t F, uint32_t &bad)
 {
     constexpr uint32_t r = E - 1015u; /* bits below the 53-bit mantissa */
     const uint64_t u = (uint64_t)F;
-    const uint64_t q = (u + ((uint64_t)1 << r >> 1)) >> r;
-    bad |= (uint32_t)((q >> 52) != 1u);
+    const uint64_t q = (u + ((uint64_t)1 << r >> 1)) >> r; /* [2^52, 2^53) if in range */
+    bad |= (uint32_t)(q >> 32) ^ (1u << 20);
     return ((uint64_t)(E - 1u) << 52) + q;
 }
 
@@ -293,14 +296,20 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
     mom.Jz = Jz;
     mom.inv = INV;
 
-    /* u = J / rho; then (e.J)^2 / rho = (e.J)(e.u) and J.J / rho = J.u, so
-     * the quadratic terms need one product per direction pair */
+    /* u = J / rho.  (e.J)^2 / rho = sum_ab e_a e_b J_a u_b, and J_a u_b =
+     * rho u_a u_b = J_b u_a, so the quadratic terms of all 18 directions
+     * come from six products: the diagonal P_aa (whose sum is J.J / rho) and
+     * the off-diagonal P_xy, P_xz, P_yz counted twice. */
     const Sp Jxs = split(Jx), Jys = split(Jy), Jzs = split(Jz);
     const int64_t ux = mul(Jxs, INVs), uy = mul(Jys, INVs), uz = mul(Jzs, INVs);
-    const int64_t Ju = mul(Jxs, split(ux)) + mul(Jys, split(uy)) + mul(Jzs, split(uz));
+    const Sp uxs = split(ux), uys = split(uy), uzs = split(uz);
+    const int64_t Pxx = mul(Jxs, uxs), Pyy = mul(Jys, uys), Pzz = mul(Jzs, uzs);
+    const int64_t Pxy2 = mul(Jxs, uys) * 2, Pxz2 = mul(Jxs, uzs) * 2,
+                  Pyz2 = mul(Jys, uzs) * 2;
+    const int64_t Ju = Pxx + Pyy + Pzz;
     const int64_t Ju15 = Ju + (Ju >> 1);
     const Sp oms = split(k.om), cfs = split(k.cf);
-    const int64_t cux = mul(cfs, split(ux));
+    const int64_t cux = mul(cfs, uxs);
     const int64_t A0 = k.om - cux, Ap = A0 + k.cf, Am = A0 - k.cf;
     const int64_t cJx = mul(cfs, Jxs), cR = mul(cfs, Rs);
     const int64_t B0 = mul(oms, split(R - kOne)) - cJx, Bp = B0 + cR, Bm = B0 - cR;
@@ -326,11 +335,16 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
         const int K = J + 1;
-        int64_t ej = 0, eu = 0;
-        if (fex(J) > 0) { ej += Jx; eu += ux; } else if (fex(J) < 0) { ej -= Jx; eu -= ux; }
-        if (fey(J) > 0) { ej += Jy; eu += uy; } else if (fey(J) < 0) { ej -= Jy; eu -= uy; }
-        if (fez(J) > 0) { ej += Jz; eu += uz; } else if (fez(J) < 0) { ej -= Jz; eu -= uz; }
-        const int64_t e2 = mul(split(ej), split(eu)); /* (e.J)^2 / rho */
+        int64_t ej = 0, e2 = 0; /* e.J and (e.J)^2 / rho */
+        if (fex(J) > 0) ej += Jx; else if (fex(J) < 0) ej -= Jx;
+        if (fey(J) > 0) ej += Jy; else if (fey(J) < 0) ej -= Jy;
+        if (fez(J) > 0) ej += Jz; else if (fez(J) < 0) ej -= Jz;
+        if (fex(J) != 0) e2 += Pxx;
+        if (fey(J) != 0) e2 += Pyy;
+        if (fez(J) != 0) e2 += Pzz;
+        if (fex(J) * fey(J) > 0) e2 += Pxy2; else if (fex(J) * fey(J) < 0) e2 -= Pxy2;
+        if (fex(J) * fez(J) > 0) e2 += Pxz2; else if (fex(J) * fez(J) < 0) e2 -= Pxz2;
+        if (fey(J) * fez(J) > 0) e2 += Pyz2; else if (fey(J) * fez(J) < 0) e2 -= Pyz2;
         const int64_t qd = e2 * 4 + (e2 >> 1) - Ju15; /* (4.5 (e.J)^2 - 1.5 J.J)/rho */
         const int64_t t3 = ej * 3;
         const int c = fcls(J);
@@ -361,7 +375,7 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
             bits[K] = to_bits(FnK, rmax);
         }
     }
-    const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u) | (fbad != 0u);
+    const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u) | ((fbad >> 20) != 0u);
     return flags | (bad ? kBad : 0u);
 }
 

@@ -143,11 +143,11 @@ __global__ void k_nbr_from_flag(const uint32_t *lexbits, const uint32_t *obits,
         uint32_t word;
         if (halfway)
             word = push ? word_base + rank_in(obits, ooffs, device_key(g, sx, sy, sz))
-                        : kBounce;
+                        : bounce_word(j, (long long)word_base + k, npad);
         else if (push && (!bounce || remote || cs > cx))
             word = word_base + rank_in(obits, ooffs, device_key(g, sx, sy, sz));
         else if (bounce)
-            word = kBounce;
+            word = bounce_word(j, (long long)word_base + k, npad);
         else
             word = rest_word;
         nbr[(long long)(j - 1) * npad + k] = word;
@@ -361,7 +361,7 @@ int flag_rank(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
         CKG(cudaStreamSynchronize(st));
         if (hbad) { rc = PLB_ERR_ARG; goto done; }
         const long long total = (long long)last_off + last_cnt;
-        if (total >= (long long)kSrcMask) { rc = PLB_ERR_ARG; goto done; }
+        if (total >= kMaxNodes) { rc = PLB_ERR_ARG; goto done; }
         *n = (int)total;
         /* slab starts: rank of the first cell of each slab (cell index is a
          * multiple of 32 only when the plane is; count the remainder) */

@@ -42,12 +42,20 @@ __host__ __device__ constexpr int wclass(int j)
     return j == 0 ? 0 : (j <= 6 ? 1 : 2);
 }
 
-/* A neighbour word: bit 31 set = bounce-back (read own node, direction
- * re(j)); else bits 0..30 = source node of the pull.  Node index N (the
- * "rest slot") holds the initial value of every direction and is never
- * written: links no push or bounce ever writes read it. */
-constexpr uint32_t kBounce = 0x80000000u;
-constexpr uint32_t kSrcMask = 0x7fffffffu;
+/* A neighbour word is the signed 32-bit offset, counted from the start of
+ * plane j of the distribution array, of the value node i pulls for
+ * direction j: the source node s (0 <= s < npad) of the pull, or for a
+ * bounce-back node i's own value of direction re(j) = j +- 1, which lies at
+ * i + (re(j) - j) * npad.  One address computation serves both.  Node index
+ * N (the "rest slot") holds the initial value of every direction and is
+ * never written: links no push or bounce ever writes read it.  Offsets need
+ * 2 * npad < 2^31, hence kMaxNodes. */
+constexpr long long kMaxNodes = (1LL << 30) - 512;
+
+__host__ __device__ inline uint32_t bounce_word(int j, long long i, long long npad)
+{
+    return (uint32_t)(i + (long long)(opp(j) - j) * npad);
+}
 
 /* Per-solve collision coefficients (host-computed from tau and F). */
 struct Coeffs {

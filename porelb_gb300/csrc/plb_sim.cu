@@ -332,11 +332,11 @@ __global__ void k_build_nbr(const plb_node_info *V, const int *perm,
         }
         uint32_t word;
         if (halfway)  /* standard rule: pull from s, or bounce if s is solid */
-            word = push ? (uint32_t)inv[sg] : kBounce;
+            word = push ? (uint32_t)inv[sg] : bounce_word(j, k, npad);
         else if (push && (!bounce || (remote_wins && ext) || sg > i))
             word = (uint32_t)inv[sg];
         else if (bounce)
-            word = kBounce;
+            word = bounce_word(j, k, npad);
         else
             word = (uint32_t)n;
         nbr[(long long)(j - 1) * npad + k] = word;
@@ -623,7 +623,7 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
         !(p->tau > 0.5) || !isfinite(p->force_x) || elem_size(p->precision) == 0 ||
         (p->ordering != PLB_ORDER_MORTON && p->ordering != PLB_ORDER_REFERENCE) ||
         (p->boundary != PLB_BOUNDARY_REFERENCE && p->boundary != PLB_BOUNDARY_HALFWAY) ||
-        n >= (int)kSrcMask)
+        n >= kMaxNodes)
         return PLB_ERR_ARG;
     if (v_sub_start[0] != 0) return PLB_ERR_NUMP;
     for (int q = 0; q < num_p; q++) {
@@ -647,10 +647,11 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->ordering = p->ordering;
     s->halo = p->halo;
     s->boundary = p->boundary;
-    /* the 80-register FP64 kernel is the faster one on GB300 (launch tuner:
-     * 12.6 vs 11.8 GLUPS at 256^3); kernel_variant 2 asks for the other */
+    /* FP64 step kernels: the 128-register one is the faster on GB300
+     * (launch tuner at 256^3: 12.9 GLUPS against 11.2 for the 80-register
+     * and 9.6 for the 64-register kernel, which spill) */
     s->variant = p->precision == PLB_FP64
-                     ? (p->kernel_variant == 2 ? 0 : (p->kernel_variant == 3 ? 3 : 1))
+                     ? (p->kernel_variant == 1 ? 1 : (p->kernel_variant == 3 ? 3 : 0))
                      : 0;
     s->block = p->block_size > 0 ? p->block_size
                                  : (p->precision == PLB_FP64 ? 128 : 256);

@@ -51,10 +51,8 @@ __device__ __forceinline__ void gather(const T *fin, const uint32_t *nbr,
     f[0] = ldg_t(fin + i);
 #pragma unroll
     for (int j = 1; j < Q; j++) {
-        const uint32_t w = __ldcs(nbr + (long long)(j - 1) * np + i);
-        const T *p = (w & kBounce) ? fin + (long long)opp(j) * np + i
-                                   : fin + (long long)j * np + (w & kSrcMask);
-        f[j] = ldg_t(p);
+        const int w = (int)__ldcs(nbr + (long long)(j - 1) * np + i);
+        f[j] = ldg_t(fin + ((long long)j * np + w));
     }
 }
 
@@ -329,8 +327,8 @@ template <> struct StoreOf<PLB_FP16DEV> { using T = __half; };
 template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
 
 /* resident blocks of 256 threads per SM the register budget is set for;
- * the FP64 form has a second variant with a tighter budget (80 registers,
- * 24 warps per SM) for the launch tuner */
+ * the FP64 form has variants with tighter budgets (80 registers, 24 warps
+ * per SM; 64 registers, 32 warps per SM) for the launch tuner */
 template <int PREC, int V> struct MinBlocks { static constexpr int v = 1; };
 template <> struct MinBlocks<PLB_FP64, 0> { static constexpr int v = 2; };
 template <> struct MinBlocks<PLB_FP64, 1> { static constexpr int v = 3; };
@@ -434,7 +432,7 @@ k_step(const StepArgs a)
 /* Batch step: CTA b works on pool block blk_list[b], which belongs to sample
  * blk_sample[pool block]. */
 template <int PREC, bool MACRO>
-__global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC, 1>::v)
+__global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC, 0>::v)
 k_batch_step(const BatchArgs a)
 {
     const int pb = a.blk_list[blockIdx.x];
