@@ -574,7 +574,7 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=80.0)
     ap.add_argument("--max-wall", type=float, default=None)
     ap.add_argument("--fp64-check", type=int, default=32)
-    ap.add_argument("--serve-precision", default="fp16dev",
+    ap.add_argument("--serve-precision", default="fp32",
                     choices=sorted(SERVE_FORMS))
     ap.add_argument("--plain-fp64", action="store_true",
                     help="also serve the same requests with the FP64 plain "

@@ -104,10 +104,11 @@ typedef struct {
     int block_size;  /* threads per block for the step kernel; 0 = default */
     int device;      /* CUDA device ordinal */
     int boundary;    /* PLB_BOUNDARY_REFERENCE (default) or PLB_BOUNDARY_HALFWAY */
-    int kernel_variant; /* PLB_FP64 only: 0 or 2 = 128-register step kernel
-                           (16 warps per SM, the default), 1 = 80-register
-                           kernel (24 warps per SM), 3 = 64-register kernel
-                           (32 warps per SM) */
+    int kernel_variant; /* register budget of the step kernel: 0 (or 2) =
+                           default (PLB_FP64: 128 registers, 16 warps per SM;
+                           FP32/16-bit forms: 48 registers); 1 = 80 registers
+                           (PLB_FP64) or unconstrained; 3 = 64 (PLB_FP64) or 40
+                           registers.  Ignored by the other FP64 forms. */
     int reserved[5];
 } plb_params;
 

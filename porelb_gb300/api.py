@@ -276,11 +276,11 @@ class Simulation:
     @classmethod
     def packed(cls, seed, nx, ny, nz, rmin, rmax, porosity, num_p=1, tau=0.8,
                force=1e-3, precision="fp64", ordering="morton", halo="auto",
-               block_size=0, device=0, boundary="reference"):
+               block_size=0, device=0, boundary="reference", kernel_variant=0):
         """Sphere pack, table and handle, all built on the device."""
         lib = _lib.load()
         p = _params(tau, force, precision, ordering, halo, block_size, device,
-                    boundary)
+                    boundary, kernel_variant)
         h = ctypes.c_void_p()
         ns = ctypes.c_int(0)
         phi = ctypes.c_double(0.0)

@@ -647,12 +647,11 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->ordering = p->ordering;
     s->halo = p->halo;
     s->boundary = p->boundary;
-    /* FP64 step kernels: the 128-register one is the faster on GB300
-     * (launch tuner at 256^3: 12.9 GLUPS against 11.2 for the 80-register
-     * and 9.6 for the 64-register kernel, which spill) */
-    s->variant = p->precision == PLB_FP64
-                     ? (p->kernel_variant == 1 ? 1 : (p->kernel_variant == 3 ? 3 : 0))
-                     : 0;
+    /* register budget of the step kernel (kernel_variant 1 and 3 are the
+     * tighter ones; for FP64 the default 128-register kernel is the faster on
+     * GB300: launch tuner at 256^3, 12.9 GLUPS against 11.2 for the
+     * 80-register and 9.6 for the 64-register kernel, which spill) */
+    s->variant = p->kernel_variant == 1 ? 1 : (p->kernel_variant == 3 ? 3 : 0);
     s->block = p->block_size > 0 ? p->block_size
                                  : (p->precision == PLB_FP64 ? 128 : 256);
     if (s->block > 256 || (s->block & 31)) s->block = 256;

@@ -326,13 +326,18 @@ template <> struct StoreOf<PLB_FP32> { using T = float; };
 template <> struct StoreOf<PLB_FP16DEV> { using T = __half; };
 template <> struct StoreOf<PLB_BF16DEV> { using T = __nv_bfloat16; };
 
-/* resident blocks of 256 threads per SM the register budget is set for;
- * the FP64 form has variants with tighter budgets (80 registers, 24 warps
- * per SM; 64 registers, 32 warps per SM) for the launch tuner */
-template <int PREC, int V> struct MinBlocks { static constexpr int v = 1; };
-template <> struct MinBlocks<PLB_FP64, 0> { static constexpr int v = 2; };
-template <> struct MinBlocks<PLB_FP64, 1> { static constexpr int v = 3; };
-template <> struct MinBlocks<PLB_FP64, 3> { static constexpr int v = 4; };
+/* Resident blocks of 256 threads per SM the register budget is set for,
+ * by kernel variant (0 = default; 1 and 3 the alternatives the launch tuner
+ * tries): fixed-point FP64 128 / 80 / 64 registers, the FP32 and 16-bit
+ * forms 48 / unconstrained / 40 registers (48 is the faster on GB300: FP16
+ * deviations 39.1 against 38.4 GLUPS at 512^3), the other FP64 forms
+ * unconstrained. */
+template <int PREC, int V> struct MinBlocks {
+    static constexpr bool dev = PREC == PLB_FP32 || PREC == PLB_FP16DEV || PREC == PLB_BF16DEV;
+    static constexpr int v = PREC == PLB_FP64 ? (V == 1 ? 3 : V == 3 ? 4 : 2)
+                           : dev ? (V == 1 ? 1 : V == 3 ? 6 : 5)
+                                 : 1;
+};
 
 /* Gather, collide and store node i.  Returns the macros; *dev_max receives
  * the largest stored deviation magnitude of the 16-bit forms. */
@@ -504,16 +509,23 @@ static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
 {
     const int grid = (a.n + block - 1) / block;
     if (grid == 0) return cudaSuccess;
-    if (PREC == PLB_FP64 && variant == 1) {
-        if (macros) k_step<PREC, true, 1><<<grid, block, 0, s>>>(a);
-        else k_step<PREC, false, 1><<<grid, block, 0, s>>>(a);
-    } else if (PREC == PLB_FP64 && variant == 3) {
-        if (macros) k_step<PREC, true, 3><<<grid, block, 0, s>>>(a);
-        else k_step<PREC, false, 3><<<grid, block, 0, s>>>(a);
-    } else {
-        if (macros) k_step<PREC, true, 0><<<grid, block, 0, s>>>(a);
-        else k_step<PREC, false, 0><<<grid, block, 0, s>>>(a);
+    /* the tighter budgets are built for the tuned forms only */
+    constexpr bool tuned = PREC == PLB_FP64 || PREC == PLB_FP32 || PREC == PLB_FP16DEV ||
+                           PREC == PLB_BF16DEV;
+    if constexpr (tuned) {
+        if (variant == 1) {
+            if (macros) k_step<PREC, true, 1><<<grid, block, 0, s>>>(a);
+            else k_step<PREC, false, 1><<<grid, block, 0, s>>>(a);
+            return cudaGetLastError();
+        }
+        if (variant == 3) {
+            if (macros) k_step<PREC, true, 3><<<grid, block, 0, s>>>(a);
+            else k_step<PREC, false, 3><<<grid, block, 0, s>>>(a);
+            return cudaGetLastError();
+        }
     }
+    if (macros) k_step<PREC, true, 0><<<grid, block, 0, s>>>(a);
+    else k_step<PREC, false, 0><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
 }
 

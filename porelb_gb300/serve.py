@@ -11,6 +11,12 @@ whose blocks the next admissions reuse.  Work of requests that arrived while
 others run overlaps on the device with theirs.
 
 Latency of a request = completion time - arrival time (wall clock).
+
+The pool's storage form defaults to FP32.  Once a sample is steady, the
+16-bit forms keep <u_x> fluctuating by about 1e-7 to 2e-6 of itself from
+one check to the next (FP32: below 4e-9), so a steady-state test tighter
+than that passes only by chance and such requests run several times longer
+in FP16 than in FP32.
 """
 import time
 
@@ -20,7 +26,7 @@ from .batch import Batch
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes, precision="fp16dev", check_every=500,
+    def __init__(self, hbm_budget_bytes, precision="fp32", check_every=500,
                  max_samples=4096, device=0, lookahead=64):
         bpn = Batch.bytes_per_node(precision)
         self.capacity = int(hbm_budget_bytes // bpn)

@@ -2,7 +2,7 @@
 node ordering.
 
 For one geometry and storage form it builds a solver per candidate
-(block size in {64, 128, 256}; for FP64 the 128-, 80- and 64-register kernels;
+(block size in {64, 128, 256}; register budgets: default, tighter, tightest;
 Morton or reference node order), times a few steps with CUDA events on the
 solver's stream after a warm-up, and keeps the fastest.  Results are cached
 per (form, boundary, node-count bucket) for the process; ``best`` returns the
@@ -48,7 +48,7 @@ def tune(flag, dims, precision="fp64", boundary="reference", steps=20):
     """Time every candidate; returns (best, [(block, ordering, variant, ms)])."""
     table = []
     n = None
-    variants = (1, 2, 3) if precision == "fp64" else (0,)
+    variants = (0, 1, 3) if precision in ("fp64", "fp32", "fp16dev", "bf16dev") else (0,)
     for ordering in ORDERINGS:
         for block in BLOCKS:
             for v in variants:
