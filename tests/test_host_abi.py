@@ -153,3 +153,24 @@ def test_create_without_device_reports_cuda_error():
     with pytest.raises(P.PorelbError) as e:
         P.Simulation(V, 2, 2, 2, vs)
     assert e.value.status == _lib.ERR_CUDA
+
+
+def test_size_limits_rejected_before_any_device_work():
+    """Neighbour words are signed offsets within two planes of the
+    distribution array, so a solve holds fewer than 2^30 - 512 nodes; sizes
+    beyond that are argument errors, found before any device call."""
+    import ctypes
+    lib = _lib.load()
+    p = _lib.Params()
+    lib.plb_default_params(ctypes.byref(p))
+    p.precision = _lib.FP16DEV
+    h = ctypes.c_void_p()
+    start = (ctypes.c_int * 1)(0)
+    V = (ctypes.c_char * 152)()
+    rc = lib.plb_create(V, (1 << 30) - 512, 1024, 1024, 1024, 1, start,
+                        ctypes.byref(p), ctypes.byref(h))
+    assert rc == _lib.ERR_ARG
+    rc = lib.plb_batch_create(ctypes.c_size_t(1 << 30), 4,
+                              _lib.FP16DEV, 500, 0, 0,
+                              ctypes.byref(h))
+    assert rc == _lib.ERR_ARG
