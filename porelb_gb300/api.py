@@ -187,9 +187,15 @@ class Simulation:
     def sync(self):
         _check(self._lib.plb_sync(self._h), "sync")
 
-    def macros(self):
-        """(Rho, Ux, Uy, Uz) of the last step in reference node order."""
-        out = np.empty((4, self.N), dtype=np.float64)
+    def macros(self, out=None):
+        """(Rho, Ux, Uy, Uz) of the last step in reference node order, into
+        `out` (a C-contiguous float64 array of shape (4, N), e.g. in pinned
+        host memory) when given."""
+        if out is None:
+            out = np.empty((4, self.N), dtype=np.float64)
+        elif (out.dtype != np.float64 or out.shape != (4, self.N) or
+              not out.flags.c_contiguous):
+            raise ValueError("out must be a C-contiguous float64 (4, N) array")
         _check(self._lib.plb_get_macros(self._h, _ptr(out[0]), _ptr(out[1]),
                                         _ptr(out[2]), _ptr(out[3])),
                "get_macros")
