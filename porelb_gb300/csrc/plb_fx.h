@@ -13,23 +13,26 @@
  * order as the reference's own rounding.
  *
  * The update is the reference's f' = (1-w) f + (w + a_j) feq_j with
- * a_j = 3 (1 - w/2) F (e_jx - u), written with rho = 1 + delta and
- * j = rho u (J_x including the half-force shift of porelb.c:347-348) as
+ * a_j = 3 (1 - w/2) F (e_jx - u), written with rho = 1 + delta, j = rho u
+ * (J_x including the half-force shift of porelb.c:347-348) and the
+ * deviations D_j = f_j - w_j as
  *
- *   f'_j = f_j - w (f_j - w_j) + G_j
- *   G_j  = w_j [ w delta + c (e_jx rho - J_x)
- *                + (w + c e_jx - c u_x) (3 e_j.J + 4.5 (e_j.J)(e_j.u) - 1.5 J.u) ]
+ *   f'_j = (1 - w) D_j + w_j + W_j + T_j q_j
+ *   W_j  = w_j [ w delta + c (e_jx rho - J_x) ]
+ *   T_j  = w_j (w + c e_jx - c u_x)
+ *   q_j  = 3 e_j.J + 4.5 (e_j.J)(e_j.u) - 1.5 J.u
  *
  * with c = 3 (1 - w/2) F, u = J/rho and w_j the lattice weights.  Every
- * term is exact algebra of the reference's expression.
+ * term is exact algebra of the reference's expression; rho = sum_j D_j +
+ * sum_j w_j and J = sum_j e_j D_j (the weights of opposite directions are
+ * equal).
  *
- * Range: collide<false> requires f_0 in [2^-8, 1) and f_j in [2^-8, 1/4)
- * for j > 0, rho in [0.5, 1.2], and results in [2^-8, 8); collide<true>
- * (constant shifts) requires every f_j, in and out, to stay in the binade of
- * its weight: f_0 in [1/4, 1/2), f_1..6 in [1/32, 1/16), f_7..18 in
- * [1/64, 1/32), i.e. deviations within -25%..+50% and -43%..+12.5% of the
- * weights.  A node outside the range is flagged and the caller recomputes it
- * in native FP64.
+ * Range: every f_j, in and out, must stay in the binade of its weight:
+ * f_0 in [1/4, 1/2), f_1..6 in [1/32, 1/16), f_7..18 in [1/64, 1/32), i.e.
+ * deviations within -25%..+50% and -43%..+12.5% of the weights, so that
+ * D_j is the difference of the FP64 bit patterns shifted by a constant and
+ * every conversion is a constant shift.  A node outside the range is
+ * flagged and the caller recomputes it in native FP64.
  *
  * The functions are host+device so that a CPU build of the same code checks
  * the integer algorithm bit for bit against the GPU.
@@ -82,15 +85,6 @@ FX_HD int64_t mul(Sp a, Sp b)
 
 FX_HD int64_t mul(int64_t a, int64_t b) { return mul(split(a), split(b)); }
 
-FX_HD uint32_t clz32(uint32_t x)
-{
-#if defined(__CUDA_ARCH__)
-    return (uint32_t)__clz((int)x);
-#else
-    return x ? (uint32_t)__builtin_clz(x) : 32u;
-#endif
-}
-
 FX_HD uint32_t f2u(float x)
 {
 #if defined(__CUDA_ARCH__)
@@ -99,27 +93,6 @@ FX_HD uint32_t f2u(float x)
     uint32_t u;
     memcpy(&u, &x, 4);
     return u;
-#endif
-}
-
-/* Exact Q60 value of a positive FP64 number given as bits.  The shift
- * s = (biased exponent - 1015) must lie in [0, smax] for f in [2^-8,
- * 2^(smax-7)); the caller checks the running maximum of s (a sign bit, zero,
- * NaN or a value out of range gives a large s). */
-FX_HD int64_t from_bits(uint64_t b, uint32_t &smax_seen)
-{
-    const uint32_t hi = (uint32_t)(b >> 32);
-    const uint32_t lo = (uint32_t)b;
-    const uint32_t s = (hi >> 20) - 1015u;
-    smax_seen = smax_seen > s ? smax_seen : s;
-    const uint32_t mh = (hi & 0xfffffu) | 0x100000u;
-    const uint32_t sh = s & 15u;
-#if defined(__CUDA_ARCH__)
-    const uint32_t oh = __funnelshift_l(lo, mh, sh);
-    const uint32_t ol = lo << sh;
-    return (int64_t)(((uint64_t)oh << 32) | ol);
-#else
-    return (int64_t)((((uint64_t)mh << 32) | lo) << sh);
 #endif
 }
 
@@ -148,29 +121,45 @@ FX_HD uint64_t to_bits(int64_t F, uint32_t &rmax_seen)
     return ((uint64_t)(ef + 867u) << 52) + q;
 }
 
-/* Fixed-binade forms: the value's biased FP64 exponent is E, the exponent
- * of its lattice weight (1/3 -> 1021, 1/18 -> 1018, 1/36 -> 1017), so every
- * shift is a constant.  A value outside that binade (input or result) sets a
- * bit at or above bit 20 of *bad (sign and exponent field XOR their expected
- * value; one three-input logic operation per value) and the whole node is
- * recomputed by the caller; bits 0..19 of *bad carry mantissa bits and mean
- * nothing. */
-template <uint32_t E>
-FX_HD int64_t from_bits_fixed(uint64_t b, uint32_t &bad)
+/* The weight classes: 1/3 (rest), 1/18 (axes), 1/36 (diagonals) as the
+ * reference's doubles (porelb.h:36-42).  kE: biased FP64 exponent of the
+ * weight; kS = kE - 1015: the shift from mantissa units to Q60; kWBits: the
+ * FP64 bits; kW: the exact Q60 value. */
+FX_HD constexpr uint32_t kE(int c) { return c == 0 ? 1021u : (c == 1 ? 1018u : 1017u); }
+FX_HD constexpr uint32_t kS(int c) { return kE(c) - 1015u; }
+FX_HD constexpr uint64_t kWBits(int c)
 {
-    bad |= (uint32_t)(b >> 32) ^ (E << 20);
-    const uint64_t m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
-    return (int64_t)(m << (E - 1015u));
+    return c == 0 ? 0x3fd5555555555555ull : (c == 1 ? 0x3fac71c71c71c71cull : 0x3f9c71c71c71c71cull);
+}
+FX_HD constexpr int64_t kW(int c)
+{
+    return (int64_t)(((kWBits(c) & 0xfffffffffffffull) | 0x10000000000000ull) << kS(c));
+}
+/* sum of the 19 weights in Q60 (2^60 - 64: the doubles sum to just below 1) */
+constexpr int64_t kWSum = kW(0) + 6 * kW(1) + 12 * kW(2);
+
+/* D = f - w_c in Q60, exactly, from the FP64 bits of f: inside the weight's
+ * binade the exponent fields cancel.  A value outside it (or negative) sets
+ * a bit at or above bit 20 of *chk (sign and exponent field XOR their
+ * expected value: one three-input logic operation); bits 0..19 of *chk
+ * carry mantissa bits and mean nothing. */
+template <int C>
+FX_HD int64_t dev_bits(uint64_t b, uint32_t &chk)
+{
+    chk |= (uint32_t)(b >> 32) ^ (kE(C) << 20);
+    return (int64_t)((b - kWBits(C)) << kS(C));
 }
 
-template <uint32_t E>
-FX_HD uint64_t to_bits_fixed(int64_t F, uint32_t &bad)
+/* FP64 bits of a class-C result whose Q60 value F already includes half a
+ * unit of the dropped bits (so the shift rounds to nearest, ties up).  A
+ * result outside the weight's binade sets a bit at or above bit 20 of
+ * *chk. */
+template <int C>
+FX_HD uint64_t out_bits(int64_t F, uint32_t &chk)
 {
-    constexpr uint32_t r = E - 1015u; /* bits below the 53-bit mantissa */
-    const uint64_t u = (uint64_t)F;
-    const uint64_t q = (u + ((uint64_t)1 << r >> 1)) >> r; /* [2^52, 2^53) if in range */
-    bad |= (uint32_t)(q >> 32) ^ (1u << 20);
-    return ((uint64_t)(E - 1u) << 52) + q;
+    const uint64_t q = (uint64_t)F >> kS(C); /* [2^52, 2^53) if in range */
+    chk |= (uint32_t)(q >> 32) ^ (1u << 20);
+    return ((uint64_t)(kE(C) - 1u) << 52) + q;
 }
 
 /* Q60 of a positive normal float in [2^-8, 4) */
@@ -184,25 +173,30 @@ FX_HD int64_t from_float(float x)
 
 /* Per-run constants (host-computed from the FP64 parameters). */
 struct Consts {
-    int64_t tp[3];      /* weights 1/3, 1/18, 1/36 as the reference's doubles */
-    int64_t om;         /* omega */
-    int64_t cf;         /* c = 3 (1 - omega/2) F */
+    Sp om1;             /* 1 - omega */
+    Sp kw;              /* w_1 omega (w_1 = 1/18) */
+    Sp kc;              /* w_1 c, c = 3 (1 - omega/2) F */
+    int64_t kwv, kcv;   /* the same two, unsplit */
+    int64_t wout[3];    /* per class: w_c + half a unit of the bits dropped */
     int64_t half_force; /* 0.5 F */
     int64_t rho_hi;     /* density guard bounds 1.2 and 0.5 */
     int64_t rho_lo;
 };
 
 /* Host: constants from the FP64 parameters.  omega = 1/tau and the weights
- * are the reference's doubles (porelb.c:88, porelb.h:36-42); each is an exact
- * multiple of 2^-60, so their Q60 images are exact. */
+ * are the reference's doubles (porelb.c:88, porelb.h:36-42). */
 static inline Consts make_consts(double tau, double force)
 {
     Consts k;
-    const double w[3] = {1.0 / 3, 1.0 / 18, 1.0 / 36};
-    for (int c = 0; c < 3; c++) k.tp[c] = (int64_t)ldexp(w[c], 60);
     const double omega = 1.0 / tau;
-    k.om = (int64_t)llround(ldexp(omega, 60));
-    k.cf = (int64_t)llround(ldexp((1.0 - 0.5 * omega) * 3.0 * force, 60));
+    const int64_t om = (int64_t)llround(ldexp(omega, 60));
+    const int64_t cf = (int64_t)llround(ldexp((1.0 - 0.5 * omega) * 3.0 * force, 60));
+    k.om1 = split(kOne - om);
+    k.kwv = mul(kW(1), om);
+    k.kcv = mul(kW(1), cf);
+    k.kw = split(k.kwv);
+    k.kc = split(k.kcv);
+    for (int c = 0; c < 3; c++) k.wout[c] = kW(c) + ((int64_t)1 << (kS(c) - 1));
     k.half_force = (int64_t)llround(ldexp(0.5 * force, 60));
     k.rho_hi = (int64_t)llround(ldexp(1.2, 60));
     k.rho_lo = (int64_t)llround(ldexp(0.5, 60));
@@ -249,30 +243,22 @@ FX_HD float rcp_rn(float x)
  * FP64, kDensity if the density guard trips.  mom receives rho*2^60, the
  * shifted momentum and 1/rho for the macro output.
  */
-template <bool FIXED>
 FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
                        Moments &mom)
 {
-    uint32_t s0 = 0, s12 = 0, rmax = 0, fbad = 0;
-    int64_t F[19];
-    if (FIXED) {
-        F[0] = from_bits_fixed<1021u>(bits[0], fbad);
+    uint32_t chk = 0;
+    int64_t D[19];
+    D[0] = dev_bits<0>(bits[0], chk);
 #pragma unroll
-        for (int j = 1; j < 19; j++)
-            F[j] = j <= 6 ? from_bits_fixed<1018u>(bits[j], fbad)
-                          : from_bits_fixed<1017u>(bits[j], fbad);
-    } else {
-        F[0] = from_bits(bits[0], s0);
-#pragma unroll
-        for (int j = 1; j < 19; j++) F[j] = from_bits(bits[j], s12);
-    }
+    for (int j = 1; j < 19; j++)
+        D[j] = j <= 6 ? dev_bits<1>(bits[j], chk) : dev_bits<2>(bits[j], chk);
 
     /* exact moments: rho and J from pair sums / differences */
-    int64_t R = F[0], Jx = 0, Jy = 0, Jz = 0;
+    int64_t R = D[0] + kWSum, Jx = 0, Jy = 0, Jz = 0;
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
-        const int64_t s = F[J] + F[J + 1];
-        const int64_t d = F[J] - F[J + 1];
+        const int64_t s = D[J] + D[J + 1];
+        const int64_t d = D[J] - D[J + 1];
         R += s;
         if (fex(J) > 0) Jx += d; else if (fex(J) < 0) Jx -= d;
         if (fey(J) > 0) Jy += d; else if (fey(J) < 0) Jy -= d;
@@ -308,30 +294,26 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
                   Pyz2 = mul(Jys, uzs) * 2;
     const int64_t Ju = Pxx + Pyy + Pzz;
     const int64_t Ju15 = Ju + (Ju >> 1);
-    const Sp oms = split(k.om), cfs = split(k.cf);
-    const int64_t cux = mul(cfs, uxs);
-    const int64_t A0 = k.om - cux, Ap = A0 + k.cf, Am = A0 - k.cf;
-    const int64_t cJx = mul(cfs, Jxs), cR = mul(cfs, Rs);
-    const int64_t B0 = mul(oms, split(R - kOne)) - cJx, Bp = B0 + cR, Bm = B0 - cR;
-    /* W = w_c * (w delta + c (e_x rho - J_x)),  T = w_c * A(e_x).  The
+
+    /* T = w_c (w + c e_x - c u_x) and W = w_c (w delta + c (e_x rho - J_x))
+     * for the 1/18 class from the per-run products w_1 w and w_1 c; the
      * reference's 1/36 is exactly half its 1/18, and its 1/3 is 6 * 1/18 to
-     * within 2^-54, so only the 1/18 products are formed. */
-    const Sp t1 = split(k.tp[1]);
-    const int64_t W10 = mul(t1, split(B0)), W1p = mul(t1, split(Bp)), W1m = mul(t1, split(Bm));
-    const int64_t W20 = W10 >> 1, W2p = W1p >> 1, W2m = W1m >> 1;
-    const int64_t W00 = W10 * 6;
-    const int64_t T10v = mul(t1, split(A0)), T1pv = mul(t1, split(Ap)), T1mv = mul(t1, split(Am));
+     * within 2^-54.  Each W also carries the class's weight and rounding
+     * half (wout), so a result is one shift away from its FP64 bits. */
+    const int64_t T10v = k.kwv - mul(k.kc, uxs);
+    const int64_t T1pv = T10v + k.kcv, T1mv = T10v - k.kcv;
     const Sp T10 = split(T10v), T1p = split(T1pv), T1m = split(T1mv);
     const Sp T20 = split(T10v >> 1), T2p = split(T1pv >> 1), T2m = split(T1mv >> 1);
     const Sp T00 = split(T10v * 6);
+    const int64_t Wv = mul(k.kw, split(R - kOne)) - mul(k.kc, Jxs);
+    const int64_t KR = mul(k.kc, Rs);
+    const int64_t W10 = Wv + k.wout[1], W1p = Wv + KR + k.wout[1], W1m = Wv - KR + k.wout[1];
+    const int64_t W20 = (Wv >> 1) + k.wout[2], W2p = ((Wv + KR) >> 1) + k.wout[2],
+                  W2m = ((Wv - KR) >> 1) + k.wout[2];
+    const int64_t W00 = Wv * 6 + k.wout[0];
 
     /* rest direction: e.J = 0 */
-    {
-        const int64_t qd = -Ju15;
-        const int64_t G = W00 + mul(T00, split(qd));
-        const int64_t Fn = F[0] - mul(oms, split(F[0] - k.tp[0])) + G;
-        bits[0] = FIXED ? to_bits_fixed<1021u>(Fn, fbad) : to_bits(Fn, rmax);
-    }
+    bits[0] = out_bits<0>(mul(k.om1, split(D[0])) + W00 + mul(T00, split(-Ju15)), chk);
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
         const int K = J + 1;
@@ -348,7 +330,6 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
         const int64_t qd = e2 * 4 + (e2 >> 1) - Ju15; /* (4.5 (e.J)^2 - 1.5 J.J)/rho */
         const int64_t t3 = ej * 3;
         const int c = fcls(J);
-        const int64_t tpc = c == 1 ? k.tp[1] : k.tp[2];
         const int eJ = fex(J), eK = fex(K);
         const int64_t WJ = c == 1 ? (eJ > 0 ? W1p : eJ < 0 ? W1m : W10)
                                   : (eJ > 0 ? W2p : eJ < 0 ? W2m : W20);
@@ -358,25 +339,17 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
                              : (eJ > 0 ? T2p : eJ < 0 ? T2m : T20);
         const Sp TK = c == 1 ? (eK > 0 ? T1p : eK < 0 ? T1m : T10)
                              : (eK > 0 ? T2p : eK < 0 ? T2m : T20);
-        const int64_t GJ = WJ + mul(TJ, split(qd + t3));
-        const int64_t GK = WK + mul(TK, split(qd - t3));
-        const int64_t FnJ = F[J] - mul(oms, split(F[J] - tpc)) + GJ;
-        const int64_t FnK = F[K] - mul(oms, split(F[K] - tpc)) + GK;
-        if (FIXED) {
-            if (c == 1) {
-                bits[J] = to_bits_fixed<1018u>(FnJ, fbad);
-                bits[K] = to_bits_fixed<1018u>(FnK, fbad);
-            } else {
-                bits[J] = to_bits_fixed<1017u>(FnJ, fbad);
-                bits[K] = to_bits_fixed<1017u>(FnK, fbad);
-            }
+        const int64_t FnJ = mul(k.om1, split(D[J])) + WJ + mul(TJ, split(qd + t3));
+        const int64_t FnK = mul(k.om1, split(D[K])) + WK + mul(TK, split(qd - t3));
+        if (c == 1) {
+            bits[J] = out_bits<1>(FnJ, chk);
+            bits[K] = out_bits<1>(FnK, chk);
         } else {
-            bits[J] = to_bits(FnJ, rmax);
-            bits[K] = to_bits(FnK, rmax);
+            bits[J] = out_bits<2>(FnJ, chk);
+            bits[K] = out_bits<2>(FnK, chk);
         }
     }
-    const bool bad = (s0 > 7u) | (s12 > 5u) | (rmax > 10u) | ((fbad >> 20) != 0u);
-    return flags | (bad ? kBad : 0u);
+    return flags | ((chk >> 20) != 0u ? kBad : 0u);
 }
 
 }  // namespace fx

@@ -289,12 +289,6 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float
 
 /* ----------------------------------------- FP64 on the integer pipes */
 
-/* constant-shift conversions with whole-node fallback (see plb_fx.h) */
-#ifndef PLB_FX_FIXED_BINADE
-#define PLB_FX_FIXED_BINADE 1
-#endif
-constexpr bool kFxFixedBinade = PLB_FX_FIXED_BINADE != 0;
-
 template <bool MACRO>
 __device__ __forceinline__ Macro collide_fx(double (&f)[Q], const Coeffs &a,
                                             bool &fallback)
@@ -303,7 +297,7 @@ __device__ __forceinline__ Macro collide_fx(double (&f)[Q], const Coeffs &a,
 #pragma unroll
     for (int j = 0; j < Q; j++) b[j] = (uint64_t)__double_as_longlong(f[j]);
     fx::Moments mm;
-    const uint32_t fl = fx::collide<kFxFixedBinade>(b, a.fxk, a.it > 0, mm);
+    const uint32_t fl = fx::collide(b, a.fxk, a.it > 0, mm);
     Macro m;
     fallback = (fl & fx::kBad) != 0;
     m.bad = (fl & fx::kDensity) != 0;

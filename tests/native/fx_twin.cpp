@@ -8,11 +8,6 @@
 
 #include "../../porelb_gb300/csrc/plb_fx.h"
 
-/* the GPU kernel's choice of conversions (plb_step.cu, PLB_FX_FIXED_BINADE) */
-#ifndef FX_TWIN_FIXED
-#define FX_TWIN_FIXED true
-#endif
-
 static const int OPP[19] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
 
 /* One pull-stream + collide step on AoS arrays (reference order), pull table
@@ -35,7 +30,7 @@ extern "C" int fx_twin_step(const uint8_t *kind, const uint32_t *src, int N,
         uint64_t b[19];
         memcpy(b, f1 + (size_t)i * 19, sizeof(b));
         plb::fx::Moments m;
-        uint32_t fl = plb::fx::collide<FX_TWIN_FIXED>(b, k, it > 0, m);
+        uint32_t fl = plb::fx::collide(b, k, it > 0, m);
         if ((fl & plb::fx::kDensity) && !(fl & plb::fx::kBad)) dens = 1;
         if (fl & plb::fx::kBad) {
             nbad++;
