@@ -39,8 +39,8 @@ class Params(ctypes.Structure):
                 ("precision", ctypes.c_int), ("ordering", ctypes.c_int),
                 ("halo", ctypes.c_int), ("block_size", ctypes.c_int),
                 ("device", ctypes.c_int), ("boundary", ctypes.c_int),
-                ("kernel_variant", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5)]
+                ("kernel_variant", ctypes.c_int), ("l2_prefetch", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class SampleParams(ctypes.Structure):

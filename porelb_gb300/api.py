@@ -124,7 +124,7 @@ def sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, device=0):
 
 
 def _params(tau, force, precision, ordering, halo, block_size, device,
-            boundary="reference", kernel_variant=0):
+            boundary="reference", kernel_variant=0, prefetch=None):
     lib = _lib.load()
     p = _lib.Params()
     lib.plb_default_params(ctypes.byref(p))
@@ -136,6 +136,7 @@ def _params(tau, force, precision, ordering, halo, block_size, device,
     p.device = device
     p.boundary = BOUNDARIES[boundary]
     p.kernel_variant = kernel_variant
+    p.l2_prefetch = 0 if prefetch is None else (1 if prefetch else -1)
     return p
 
 
@@ -147,7 +148,7 @@ class Simulation:
     def __init__(self, V, nx, ny, nz, v_sub_start=None, tau=0.8,
                  force=1e-3, precision="fp64_exact", ordering="morton",
                  halo="auto", block_size=0, device=0, boundary="reference",
-                 kernel_variant=0):
+                 kernel_variant=0, prefetch=None):
         self._lib = _lib.load()
         self.V = np.ascontiguousarray(V, dtype=NODE_DTYPE)
         self.nx, self.ny, self.nz = nx, ny, nz
@@ -157,7 +158,7 @@ class Simulation:
         self.tau, self.force = float(tau), float(force)
         self.precision = precision
         p = _params(tau, force, precision, ordering, halo, block_size, device,
-                    boundary, kernel_variant)
+                    boundary, kernel_variant, prefetch)
         h = ctypes.c_void_p()
         _check(self._lib.plb_create(_ptr(self.V), len(self.V), nx, ny, nz,
                                     self.num_p, _iptr(self.v_sub_start),
@@ -265,14 +266,14 @@ class Simulation:
     def from_flag(cls, flag, nx, ny, nz, num_p=1, tau=0.8, force=1e-3,
                   precision="fp64_exact", ordering="morton", halo="auto",
                   block_size=0, device=0, boundary="reference",
-                  kernel_variant=0):
+                  kernel_variant=0, prefetch=None):
         """build_V + create on the device from a 0/1 flag grid."""
         lib = _lib.load()
         flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
         if flag.size != nx * ny * nz:
             raise ValueError("flag size does not match nx*ny*nz")
         p = _params(tau, force, precision, ordering, halo, block_size, device,
-                    boundary, kernel_variant)
+                    boundary, kernel_variant, prefetch)
         h = ctypes.c_void_p()
         _check(lib.plb_create_from_flag(_ptr(flag), nx, ny, nz, num_p,
                                         ctypes.byref(p), ctypes.byref(h)),
@@ -282,11 +283,12 @@ class Simulation:
     @classmethod
     def packed(cls, seed, nx, ny, nz, rmin, rmax, porosity, num_p=1, tau=0.8,
                force=1e-3, precision="fp64", ordering="morton", halo="auto",
-               block_size=0, device=0, boundary="reference", kernel_variant=0):
+               block_size=0, device=0, boundary="reference", kernel_variant=0,
+               prefetch=None):
         """Sphere pack, table and handle, all built on the device."""
         lib = _lib.load()
         p = _params(tau, force, precision, ordering, halo, block_size, device,
-                    boundary, kernel_variant)
+                    boundary, kernel_variant, prefetch)
         h = ctypes.c_void_p()
         ns = ctypes.c_int(0)
         phi = ctypes.c_double(0.0)

@@ -81,6 +81,7 @@ struct StepArgs {
     double *partial;  /* [2][gridDim.x]: sum ux, sum rho */
     unsigned long long *err; /* min over (it << 32 | reference index) */
     unsigned int *flags;     /* bit 0: FP16 scale overflow, bit 1: fallback */
+    int pf_blocks;           /* L2 prefetch distance in blocks (0 = none) */
 };
 
 /* One sample of a batch (device copy). */
@@ -125,6 +126,8 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
                 uint32_t rest_word, cudaStream_t st);
 
 /* Launch one step of the given precision. */
+/* blocks of the step kernel resident on the device at once (0 if unknown) */
+int step_wave_blocks(int precision, int block, int variant);
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
                         int block, int variant, cudaStream_t s);
 

@@ -27,6 +27,7 @@ struct plb_sim {
     int n, nx, ny, nz, num_p;
     long long npad;
     int precision, ordering, halo, block, boundary, variant;
+    int prefetch, wave; /* L2 prefetch on; resident blocks (0 = not queried) */
     int device;
     cudaStream_t stream;
     void *f[2];
@@ -655,6 +656,10 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->block = p->block_size > 0 ? p->block_size
                                  : (p->precision == PLB_FP64 ? 128 : 256);
     if (s->block > 256 || (s->block & 31)) s->block = 256;
+    /* prefetching the next wave into L2 pays for the issue-bound FP64 form
+     * (+5% at 256^3 and 512^3) and costs the bandwidth-bound forms (FP32
+     * -13%, FP16 deviations up to -11%) */
+    s->prefetch = p->l2_prefetch > 0 || (p->l2_prefetch == 0 && p->precision == PLB_FP64);
     s->device = p->device;
     s->elem = elem_size(p->precision);
     s->tau = p->tau;
@@ -905,6 +910,8 @@ int plb_step_async(plb_sim *s, int it_begin, int nsteps)
     a.partial = s->partial;
     a.err = s->err;
     a.flags = s->flags;
+    if (s->prefetch && s->wave == 0) s->wave = step_wave_blocks(s->precision, s->block, s->variant);
+    a.pf_blocks = s->prefetch ? s->wave : 0;
     for (int k = 0; k < nsteps; k++) {
         a.fin = s->f[s->cur];
         a.fout = s->f[s->cur ^ 1];

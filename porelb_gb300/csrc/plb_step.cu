@@ -382,11 +382,46 @@ __device__ __forceinline__ Macro step_node(const void *fin_, void *fout_,
     return m;
 }
 
+/* Bulk L2 prefetch of [p, p + bytes), bytes a positive multiple of 16 and
+ * p 16-byte aligned. */
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+/* Thread 0 of a block asks L2 for the node range of block b (the block that
+ * will run on this SM about when this one ends): its 18 rows of neighbour
+ * words and its 19 rows of distributions.  In Morton order most gathers of
+ * that block read inside the ranges of the blocks of the same wave, so its
+ * loads then wait for L2 instead of DRAM.  Rows are npad elements (a
+ * multiple of 64) and the block size is a multiple of 32, so every range
+ * starts 64-byte aligned and spans a multiple of 64 bytes inside its row. */
+template <typename T>
+__device__ __forceinline__ void prefetch_block(const T *fin, const uint32_t *nbr,
+                                               long long np, long long n, long long b,
+                                               int bs)
+{
+    const long long i0 = b * bs;
+    if (i0 >= n) return;
+    const long long cnt = np - i0 < bs ? np - i0 : bs;
+    const unsigned wb = (unsigned)(cnt * 4);
+    const unsigned fb = (unsigned)(cnt * (long long)sizeof(T));
+#pragma unroll 1
+    for (int j = 0; j < Q - 1; j++) prefetch_l2(nbr + (long long)j * np + i0, wb);
+#pragma unroll 1
+    for (int j = 0; j < Q; j++) prefetch_l2(fin + (long long)j * np + i0, fb);
+}
+
 template <int PREC, bool MACRO, int VARIANT>
 __global__ void __launch_bounds__(256, MinBlocks<PREC, VARIANT>::v)
 k_step(const StepArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.pf_blocks > 0 && threadIdx.x == 0)
+        prefetch_block<typename StoreOf<PREC>::T>((const typename StoreOf<PREC>::T *)a.fin,
+                                                  a.nbr, a.npad, a.n,
+                                                  (long long)blockIdx.x + a.pf_blocks,
+                                                  blockDim.x);
     double sum_u = 0.0, sum_r = 0.0;
     if (i < a.n) {
         float dm = 0.f;
@@ -521,6 +556,39 @@ static cudaError_t launch_prec(bool macros, const StepArgs &a, int block,
     if (macros) k_step<PREC, true, 0><<<grid, block, 0, s>>>(a);
     else k_step<PREC, false, 0><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+/* Blocks of the (non-macro) step kernel resident on the whole device at
+ * once: the L2 prefetch distance. */
+template <int PREC>
+static int wave_prec(int block, int variant)
+{
+    const void *fn = (const void *)k_step<PREC, false, 0>;
+    constexpr bool tuned = PREC == PLB_FP64 || PREC == PLB_FP32 || PREC == PLB_FP16DEV ||
+                           PREC == PLB_BF16DEV;
+    if constexpr (tuned) {
+        if (variant == 1) fn = (const void *)k_step<PREC, false, 1>;
+        if (variant == 3) fn = (const void *)k_step<PREC, false, 3>;
+    }
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0) != cudaSuccess)
+        return 0;
+    return sms * per;
+}
+
+int step_wave_blocks(int precision, int block, int variant)
+{
+    switch (precision) {
+    case PLB_FP64_EXACT: return wave_prec<PLB_FP64_EXACT>(block, variant);
+    case PLB_FP64: return wave_prec<PLB_FP64>(block, variant);
+    case PLB_FP64_FMA: return wave_prec<PLB_FP64_FMA>(block, variant);
+    case PLB_FP32: return wave_prec<PLB_FP32>(block, variant);
+    case PLB_FP16DEV: return wave_prec<PLB_FP16DEV>(block, variant);
+    case PLB_BF16DEV: return wave_prec<PLB_BF16DEV>(block, variant);
+    default: return 0;
+    }
 }
 
 template <int PREC>

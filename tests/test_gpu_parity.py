@@ -158,25 +158,45 @@ def test_fp64_fixed_point_within_1e12_high_velocity(case):
 
 @pytest.mark.parametrize("dims", [(96, 96, 96), (12, 10, 9)])
 def test_fp64_kernel_variants_agree_bitwise(dims):
-    """Every FP64 step kernel (128-, 80- and 64-register) runs the same
-    integer collision: distributions, macros and permeability agree bit for
-    bit."""
+    """Every FP64 step kernel (128-, 80- and 64-register, with and without
+    the L2 prefetch) runs the same integer collision: distributions, macros
+    and permeability agree bit for bit."""
     flag = pack_flag(dims, 11, 3.0, 6.0, 0.4)
     runs = {}
-    for v in (0, 1, 2, 3):
+    for v in (0, 1, 2, 3, "off"):
         sim = P.Simulation.from_flag(flag, *dims, tau=0.7, force=1e-4,
-                                     precision="fp64", kernel_variant=v)
+                                     precision="fp64",
+                                     kernel_variant=0 if v == "off" else v,
+                                     prefetch=False if v == "off" else None)
         sim.init_dist_macro()
         sim.step(7)
         sim.step(6, it_begin=7)
         runs[v] = (sim.get_f(), sim.macros(), sim.permeability()[0])
         sim.close()
     f1, m1, k1 = runs[0]
-    for v in (1, 2, 3):
+    for v in (1, 2, 3, "off"):
         f, m, k = runs[v]
         assert (f == f1).all(), v
         assert all((a == b).all() for a, b in zip(m, m1)), v
         assert k == k1, v
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16dev"])
+def test_prefetch_changes_no_result(precision):
+    """The L2 prefetch (off by default for the deviation forms) moves no
+    value: forced on, the results are the same bits."""
+    dims = (64, 48, 40)
+    flag = pack_flag(dims, 12, 3.0, 6.0, 0.4)
+    out = []
+    for pf in (None, True):
+        sim = P.Simulation.from_flag(flag, *dims, tau=0.9, force=1e-4,
+                                     precision=precision, prefetch=pf)
+        sim.init_dist_macro()
+        sim.step(9)
+        out.append((sim.get_f(), sim.macros()))
+        sim.close()
+    assert (out[0][0] == out[1][0]).all()
+    assert all((a == b).all() for a, b in zip(out[0][1], out[1][1]))
 
 
 def test_set_get_roundtrip_and_restart():
