@@ -911,7 +911,9 @@ int plb_step_async(plb_sim *s, int it_begin, int nsteps)
     a.err = s->err;
     a.flags = s->flags;
     if (s->prefetch && s->wave == 0) s->wave = step_wave_blocks(s->precision, s->block, s->variant);
-    a.pf_blocks = s->prefetch ? s->wave : 0;
+    /* half a wave of resident blocks ahead (measured at 256^3 and 512^3:
+     * +0.7% against a whole wave, +7% against no prefetch) */
+    a.pf_blocks = s->prefetch ? (s->wave + 1) / 2 : 0;
     for (int k = 0; k < nsteps; k++) {
         a.fin = s->f[s->cur];
         a.fout = s->f[s->cur ^ 1];

@@ -389,11 +389,11 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-/* Thread 0 of a block asks L2 for the node range of block b (the block that
- * will run on this SM about when this one ends): its 18 rows of neighbour
- * words and its 19 rows of distributions.  In Morton order most gathers of
- * that block read inside the ranges of the blocks of the same wave, so its
- * loads then wait for L2 instead of DRAM.  Rows are npad elements (a
+/* Thread 0 of a block asks L2 for the node range of block b (a block that
+ * starts some time after this one, pf_blocks blocks later in launch order):
+ * its 18 rows of neighbour words and its 19 rows of distributions.  In
+ * Morton order most gathers of that block read inside the ranges of the
+ * blocks launched near it, so its loads then wait for L2 instead of DRAM.  Rows are npad elements (a
  * multiple of 64) and the block size is a multiple of 32, so every range
  * starts 64-byte aligned and spans a multiple of 64 bytes inside its row. */
 template <typename T>
