@@ -180,14 +180,33 @@ def run_reference(args, rank, world):
     cores = host_threads()
     p = slab_count(dims[2], cores)
     V, vs = P.build_table(flag, *dims, p)
+    # one oracle solve for the whole run: W single warm-up steps, then K
+    # bench steps of `per` lattice steps each, `per` sized so that the K
+    # steps take about --ref-budget seconds in all
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    s = oracle_py.OracleSim(V, *dims, vs, w["tau"], w["force"])
+    s.init()
+    it = 0
+    t0 = time.perf_counter()
+    s.run(1, threads=p, it_begin=it)
+    it += 1
+    one = time.perf_counter() - t0
     for _ in range(args.warmup):
-        cpu_port_mlups(V, vs, dims, w, 1.0, p)
+        s.run(1, threads=p, it_begin=it)
+        it += 1
+    per = max(1, int(args.ref_budget / max(args.steps, 1) / max(one, 1e-6)))
     vals = []
-    detail = None
+    total = 0.0
     for _ in range(args.steps):
-        v, steps, el = cpu_port_mlups(V, vs, dims, w, args.cpu_budget, p)
-        vals.append(v)
-        detail = (steps, el)
+        t0 = time.perf_counter()
+        s.run(per, threads=p, it_begin=it)
+        el = time.perf_counter() - t0
+        it += per
+        total += el
+        vals.append(len(V) * per / el / 1e6)
+    s.close()
+    detail = (per, total)
     value = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3),
@@ -199,9 +218,10 @@ def run_reference(args, rank, world):
                    "tau": w["tau"], "force": w["force"]},
         "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS",
                          "cores": p, "kind": "port",
-                         "sample": f"{detail[0]} lattice steps of the full "
-                                   f"workload per bench step ({detail[1]:.1f} s),"
-                                   f" {p} z-slab ranks on {p} threads"},
+                         "sample": f"{detail[0]} lattice step(s) of the full "
+                                   f"workload per bench step, {args.steps} bench "
+                                   f"steps ({detail[1]:.1f} s in all), {p} z-slab "
+                                   f"ranks on {p} threads"},
         "e2e": {"value": round(value, 3), "unit": "MLUPS",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -601,7 +621,10 @@ def main():
                          "(0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--e2e-reps", type=int, default=2)
-    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--cpu-budget", type=float, default=10.0,
+                    help="seconds of the GPU arm's CPU-baseline sample")
+    ap.add_argument("--ref-budget", type=float, default=60.0,
+                    help="seconds of CPU work in all for --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mode", default="plain",
                     choices=["plain", "batched", "served", "precision"])
