@@ -64,8 +64,22 @@ struct Sp {
 FX_HD Sp split(int64_t a)
 {
     Sp s;
+#if defined(__CUDA_ARCH__)
+    /* t = bits 30-31 of the low word; h = 4 hi + t and l = lo - t 2^30 as
+     * two integer multiply-adds: the GPU's ALU pipe is the busier one in
+     * the collision, the multiply-add pipe has room (and the compiler's own
+     * form of the 64-bit shift and mask costs more instructions). */
+    const uint32_t lo = (uint32_t)a, hi = (uint32_t)((uint64_t)a >> 32);
+    const uint32_t t = lo >> 30;
+    int32_t h, l;
+    asm("mad.lo.s32 %0, %1, 4, %2;" : "=r"(h) : "r"(hi), "r"(t));
+    asm("mad.lo.s32 %0, %1, -1073741824, %2;" : "=r"(l) : "r"(t), "r"(lo));
+    s.h = h;
+    s.l = l;
+#else
     s.h = (int32_t)(a >> 30);
     s.l = (int32_t)((uint32_t)a & 0x3fffffffu);
+#endif
     return s;
 }
 
