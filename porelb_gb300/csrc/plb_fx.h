@@ -99,6 +99,17 @@ FX_HD int64_t mul(Sp a, Sp b)
 
 FX_HD int64_t mul(int64_t a, int64_t b) { return mul(split(a), split(b)); }
 
+/* a * b + c * d (all Q60, magnitudes < 2) with one shared shift: the four
+ * middle products are summed before the shift (|sum| < 2^63), and the
+ * constant 2^30 is the rounding half plus the means (1/4 each) of the two
+ * dropped low x low terms.  |error| <= 1 unit of 2^-60. */
+FX_HD int64_t mul2(Sp a, Sp b, Sp c, Sp d)
+{
+    const int64_t mid = wmul(a.h, b.l) + wmul(a.l, b.h) + wmul(c.h, d.l) + wmul(c.l, d.h) +
+                        ((int64_t)1 << 30);
+    return wmul(a.h, b.h) + wmul(c.h, d.h) + (mid >> 30);
+}
+
 FX_HD uint32_t f2u(float x)
 {
 #if defined(__CUDA_ARCH__)
@@ -327,7 +338,7 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
     const int64_t W00 = Wv * 6 + k.wout[0];
 
     /* rest direction: e.J = 0 */
-    bits[0] = out_bits<0>(mul(k.om1, split(D[0])) + W00 + mul(T00, split(-Ju15)), chk);
+    bits[0] = out_bits<0>(mul2(k.om1, split(D[0]), T00, split(-Ju15)) + W00, chk);
 #pragma unroll
     for (int J = 1; J < 19; J += 2) {
         const int K = J + 1;
@@ -353,8 +364,8 @@ FX_HD uint32_t collide(uint64_t (&bits)[19], const Consts &k, bool it_pos,
                              : (eJ > 0 ? T2p : eJ < 0 ? T2m : T20);
         const Sp TK = c == 1 ? (eK > 0 ? T1p : eK < 0 ? T1m : T10)
                              : (eK > 0 ? T2p : eK < 0 ? T2m : T20);
-        const int64_t FnJ = mul(k.om1, split(D[J])) + WJ + mul(TJ, split(qd + t3));
-        const int64_t FnK = mul(k.om1, split(D[K])) + WK + mul(TK, split(qd - t3));
+        const int64_t FnJ = mul2(k.om1, split(D[J]), TJ, split(qd + t3)) + WJ;
+        const int64_t FnK = mul2(k.om1, split(D[K]), TK, split(qd - t3)) + WK;
         if (c == 1) {
             bits[J] = out_bits<1>(FnJ, chk);
             bits[K] = out_bits<1>(FnK, chk);
