@@ -109,7 +109,8 @@ typedef struct {
                            FP32/16-bit forms: 48 registers); 1 = 80 registers
                            (PLB_FP64) or unconstrained; 3 = 64 (PLB_FP64) or 40
                            registers.  Ignored by the other FP64 forms. */
-    int l2_prefetch; /* L2 prefetch of the nodes of the next wave of blocks:
+    int l2_prefetch; /* L2 prefetch of the nodes of the blocks half a wave
+                        of resident blocks ahead:
                         0 = the form's default (on for PLB_FP64, where it
                         pays; off for the bandwidth-bound forms), 1 = on,
                         -1 = off */
