@@ -53,3 +53,26 @@ def test_reference_arm_silent_off_rank0(monkeypatch, capsys):
     monkeypatch.setenv("WORLD_SIZE", "2")
     bench.main()
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_on_rank0(monkeypatch, capsys):
+    """The reference arm's JSON line: the contract's keys, its CPU work
+    bounded by --ref-budget whatever --steps is."""
+    import json
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--workload",
+                                      "c1_64", "--steps", "50", "--warmup", "3",
+                                      "--ref-budget", "2"])
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    t0 = time.perf_counter()
+    bench.main()
+    took = time.perf_counter() - t0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "fluid MLUPS"
+    assert line["value"] > 0 and line["unit"] == "MLUPS" and line["steps"] == 50
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert took < 60
