@@ -649,9 +649,9 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->halo = p->halo;
     s->boundary = p->boundary;
     /* register budget of the step kernel (kernel_variant 1 and 3 are the
-     * tighter ones; for FP64 the default 128-register kernel is the faster on
-     * GB300: launch tuner at 256^3, 12.9 GLUPS against 11.2 for the
-     * 80-register and 9.6 for the 64-register kernel, which spill) */
+     * alternatives; for FP64 the default 128-register kernel is the faster on
+     * GB300 - every tighter budget spills: 96 to 120 registers ran at 13.5 to
+     * 15.2 GLUPS at 256^3 against 16.2) */
     s->variant = p->kernel_variant == 1 ? 1 : (p->kernel_variant == 3 ? 3 : 0);
     s->block = p->block_size > 0 ? p->block_size
                                  : (p->precision == PLB_FP64 ? 128 : 256);
