@@ -1,0 +1,76 @@
+"""Parity at the full size of the 256^3 plain-FP64 workload (seed 1,
+R ~ U[4, 10], porosity 0.35, tau 0.8, F 5e-7; 5.87M fluid nodes), through
+properties that do not depend on size:
+
+* the bit-exact form against the oracle run as 16 z-slab ranks (the
+  reference's own multi-rank semantics, as mpirun -np 16 would run it);
+* the fixed-point FP64 form within 1e-12 of the same oracle state;
+* the device-built table (from the flag grid) against the host-built table
+  (preprocess's build_V): the same bits after a few steps;
+* mass conservation of the half-way bounce-back at full size."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+import porelb_gb300 as P
+
+from helpers import max_rel
+
+pytestmark = pytest.mark.gpu
+DIMS = (256, 256, 256)
+TAU, FORCE = 0.8, 5e-7
+
+
+@pytest.fixture(scope="module")
+def c2():
+    flag, _, _ = P.sphere_pack(1, *DIMS, 4.0, 10.0, 0.35)
+    return flag
+
+
+def test_c2_exact_and_fixed_point_against_16_rank_oracle(c2):
+    V, vs = P.build_table(c2, *DIMS, 16)
+    steps = 6
+    s = O.OracleSim(V, *DIMS, vs, TAU, FORCE)
+    s.init()
+    assert s.run(steps, threads=min(16, os.cpu_count() or 1))[0] == 0
+    ref = s.f0()
+    ref_rho = s.macros()[0]
+    s.close()
+    with P.Simulation(V, *DIMS, vs, tau=TAU, force=FORCE, precision="fp64_exact") as sim:
+        sim.init_dist_macro()
+        sim.step(steps)
+        assert (sim.get_f() == ref).all()
+        assert (sim.macros()[0] == ref_rho).all()
+    with P.Simulation(V, *DIMS, vs, tau=TAU, force=FORCE, precision="fp64") as sim:
+        sim.init_dist_macro()
+        sim.step(steps)
+        assert max_rel(sim.get_f(), ref) <= 1e-12
+
+
+def test_c2_device_table_equals_host_table(c2):
+    V, vs = P.build_table(c2, *DIMS, 1)
+    out = []
+    for make in (lambda: P.Simulation(V, *DIMS, vs, tau=TAU, force=FORCE,
+                                      precision="fp64_exact"),
+                 lambda: P.Simulation.from_flag(c2, *DIMS, tau=TAU, force=FORCE,
+                                                precision="fp64_exact")):
+        with make() as sim:
+            sim.init_dist_macro()
+            sim.step(4)
+            out.append((sim.get_f(), sim.macros()))
+    assert (out[0][0] == out[1][0]).all()
+    assert all((a == b).all() for a, b in zip(out[0][1], out[1][1]))
+
+
+def test_c2_halfway_conserves_mass(c2):
+    with P.Simulation.from_flag(c2, *DIMS, tau=TAU, force=FORCE, precision="fp64",
+                                boundary="halfway") as sim:
+        sim.init_dist_macro()
+        sim.step(1)
+        _, m0 = sim.reduce()
+        sim.step(300, it_begin=1)
+        _, m1 = sim.reduce()
+        assert abs(m1 - m0) <= 1e-12 * m0
+        assert abs(m0 - sim.N) <= 1e-9 * sim.N
