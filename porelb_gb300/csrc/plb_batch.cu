@@ -78,10 +78,14 @@ __global__ void k_fill_rest(void *f0, void *f1, long long npad, long long lo,
     }
 }
 
-__global__ void k_set_blocks(int *blk, long long lo, long long cnt, int v)
+/* block map of pool blocks [lo, lo + cnt): sample sid (<< 9) and the
+ * number of its `nodes` that fall in each block; sid < 0 frees them */
+__global__ void k_set_blocks(int *blk, long long lo, long long cnt, int sid, long long nodes)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < cnt) blk[lo + k] = v;
+    if (k >= cnt) return;
+    const long long in = nodes - k * B;
+    blk[lo + k] = sid < 0 ? -1 : (sid << 9) | (int)(in < B ? (in > 0 ? in : 0) : B);
 }
 
 __global__ void k_advance(int *t, int by) { *t += by; }
@@ -89,14 +93,15 @@ __global__ void k_advance(int *t, int by) { *t += by; }
 /* per-sample sums of the per-block partials, in block order (one CTA per
  * sample slot): ssum[s] = {sum ux, sum rho, max |stored deviation|} */
 __global__ void k_sample_sums(const SampleDev *sp, const int *active,
-                              const double *partial, int nb, double *ssum)
+                              const double *partial, int nb, int h, double *ssum)
 {
     const int s = blockIdx.x;
     __shared__ double su[32], sr[32], sd[32];
     double tu = 0.0, tr = 0.0, td = 0.0;
     if (active[s]) {
-        const long long b0 = sp[s].base / B;
-        const long long b1 = (sp[s].base + sp[s].n + B - 1) / B;
+        /* h partial rows per pool block, nb rows in all */
+        const long long b0 = sp[s].base / B * h;
+        const long long b1 = (sp[s].base + sp[s].n + B - 1) / B * h;
         for (long long b = b0 + threadIdx.x; b < b1 && b < nb; b += blockDim.x) {
             tu += partial[b];
             tr += partial[nb + b];
@@ -283,7 +288,8 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
 {
     if (!out) return PLB_ERR_ARG;
     *out = nullptr;
-    if (capacity_nodes == 0 || max_samples <= 0 || elem_of(precision) == 0 ||
+    if (capacity_nodes == 0 || max_samples <= 0 || max_samples > (1 << 22) ||
+        elem_of(precision) == 0 ||
         check_every <= 0 || (check_every & 1) || capacity_nodes >= (size_t)kMaxNodes - B)
         return PLB_ERR_ARG;
     int ndev = 0;
@@ -318,7 +324,7 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
     al(&b->blist, 4 * (size_t)b->cap_blocks);
     al(&b->sdev, sizeof(SampleDev) * (size_t)max_samples);
     al(&b->sactive, 4 * (size_t)max_samples);
-    al(&b->partial, 8 * 3 * (size_t)b->cap_blocks);
+    al(&b->partial, 8 * 3 * 2 * (size_t)b->cap_blocks);
     al(&b->ssum, 8 * 3 * (size_t)max_samples);
     al(&b->serr, 4 * (size_t)max_samples);
     al(&b->t_dev, 4);
@@ -328,7 +334,7 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
     if (e == cudaSuccess) e = cudaMemsetAsync(b->sactive, 0, 4 * (size_t)max_samples, b->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->serr, 0, 4 * (size_t)max_samples, b->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->t_dev, 0, 4, b->st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->partial, 0, 8 * 3 * (size_t)b->cap_blocks, b->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->partial, 0, 8 * 3 * 2 * (size_t)b->cap_blocks, b->st);
     if (e == cudaSuccess) {
         k_fill_rest<<<1, B, 0, b->st>>>(b->f[0], b->f[1], b->npad, b->rest, b->rest + 1,
                                         (int)b->elem);
@@ -444,7 +450,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     if (n > 0)
         k_fill_rest<<<gb(n, B), B, 0, b->st>>>(b->f[0], b->f[1], b->npad, d.base, d.base + n,
                                               (int)b->elem);
-    k_set_blocks<<<gb(nblk, B), B, 0, b->st>>>(b->blk, blk0, nblk, sid);
+    k_set_blocks<<<gb(nblk, B), B, 0, b->st>>>(b->blk, blk0, nblk, sid, n);
     BCK(cudaGetLastError());
     BCK(cudaStreamSynchronize(b->st));
     b->list_dirty = true;
@@ -511,7 +517,10 @@ static int build_graph(plb_batch *b)
     a.nbr = b->nbr;
     a.npad = b->npad;
     a.blk_list = b->blist;
-    a.part_stride = b->cap_blocks;
+    /* the FP64 form prefetches the pool block half a wave of CTAs ahead */
+    a.pf_blocks = b->precision == PLB_FP64 ? (batch_wave_blocks(b->precision) + 1) / 2 : 0;
+    const int h = batch_ctas_per_block(b->precision);
+    a.part_stride = h * b->cap_blocks;
     a.blk_sample = b->blk;
     a.samples = b->sdev;
     a.t_base = b->t_dev;
@@ -530,7 +539,7 @@ static int build_graph(plb_batch *b)
     if (e == cudaSuccess) {
         k_advance<<<1, 1, 0, b->st>>>(b->t_dev, b->K);
         k_sample_sums<<<b->max_samples, 128, 0, b->st>>>(b->sdev, b->sactive, b->partial,
-                                                         (int)b->cap_blocks, b->ssum);
+                                                         (int)(h * b->cap_blocks), h, b->ssum);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -559,7 +568,7 @@ static void retire(plb_batch *b, int sid, int status)
     h.status = status;
     const int zero = 0;
     cudaMemcpyAsync(b->sactive + sid, &zero, 4, cudaMemcpyHostToDevice, b->st);
-    k_set_blocks<<<gb(h.nblk, B), B, 0, b->st>>>(b->blk, h.blk0, h.nblk, -1);
+    k_set_blocks<<<gb(h.nblk, B), B, 0, b->st>>>(b->blk, h.blk0, h.nblk, -1, 0);
     free_range(b, h.blk0, h.nblk);
     b->list_dirty = true;
     b->done.push_back(sid);

@@ -98,7 +98,8 @@ struct BatchArgs {
     const uint32_t *nbr;
     long long npad;
     const int *blk_list;       /* pool blocks this launch covers (one CTA each) */
-    const int *blk_sample;     /* sample of every 256-node pool block, -1 = free */
+    const int *blk_sample;     /* per 256-node pool block: sample << 9 | nodes of
+                                  the sample in the block, -1 = free */
     long long part_stride;     /* pool blocks: stride of the partial-sum rows */
     const SampleDev *samples;
     const int *t_base;         /* batch step counter (device) */
@@ -107,6 +108,7 @@ struct BatchArgs {
     double *partial;           /* [3][part_stride] by pool block: sum ux, sum rho,
                                   max |stored deviation| */
     unsigned int *serr;        /* per-sample error bits */
+    int pf_blocks;             /* L2 prefetch distance in CTAs (0 = none) */
 };
 
 /* Exclusive scan of m uint32 counts into offs (device memory). */
@@ -128,6 +130,11 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
 /* Launch one step of the given precision. */
 /* blocks of the step kernel resident on the device at once (0 if unknown) */
 int step_wave_blocks(int precision, int block, int variant);
+/* the same for the batch step kernel */
+int batch_wave_blocks(int precision);
+/* CTAs of the batch step per 256-node pool block (partial-sum rows per
+ * pool block) */
+int batch_ctas_per_block(int precision);
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
                         int block, int variant, cudaStream_t s);
 

@@ -335,17 +335,13 @@ template <int PREC, int V> struct MinBlocks {
 
 /* Gather, collide and store node i.  Returns the macros; *dev_max receives
  * the largest stored deviation magnitude of the 16-bit forms. */
-template <int PREC, bool MACRO>
-__device__ __forceinline__ Macro step_node(const void *fin_, void *fout_,
-                                           const uint32_t *nbr, long long np,
-                                           long long i, const Coeffs &co,
-                                           unsigned int &flags, float &dev_max)
+/* Collide node i's streamed values raw[] and store them. */
+template <int PREC, bool MACRO, typename T>
+__device__ __forceinline__ Macro collide_node(T (&raw)[Q], const T *fin, T *fout,
+                                              const uint32_t *nbr, long long np,
+                                              long long i, const Coeffs &co,
+                                              unsigned int &flags, float &dev_max)
 {
-    using T = typename StoreOf<PREC>::T;
-    const T *fin = (const T *)fin_;
-    T *fout = (T *)fout_;
-    T raw[Q];
-    gather<T>(fin, nbr, np, i, raw);
     Macro m;
     if constexpr (PREC == PLB_FP64) {
         bool fallback;
@@ -380,6 +376,21 @@ __device__ __forceinline__ Macro step_node(const void *fin_, void *fout_,
         dev_max = big;
     }
     return m;
+}
+
+/* Gather, collide and store node i.  Returns the macros; dev_max receives
+ * the largest stored deviation magnitude of the 16-bit forms. */
+template <int PREC, bool MACRO>
+__device__ __forceinline__ Macro step_node(const void *fin_, void *fout_,
+                                           const uint32_t *nbr, long long np,
+                                           long long i, const Coeffs &co,
+                                           unsigned int &flags, float &dev_max)
+{
+    using T = typename StoreOf<PREC>::T;
+    const T *fin = (const T *)fin_;
+    T raw[Q];
+    gather<T>(fin, nbr, np, i, raw);
+    return collide_node<PREC, MACRO>(raw, fin, (T *)fout_, nbr, np, i, co, flags, dev_max);
 }
 
 /* Bulk L2 prefetch of [p, p + bytes), bytes a positive multiple of 16 and
@@ -465,14 +476,31 @@ k_step(const StepArgs a)
 
 /* Batch step: CTA b works on pool block blk_list[b], which belongs to sample
  * blk_sample[pool block]. */
-template <int PREC, bool MACRO>
-__global__ void __launch_bounds__(kBatchBlock, MinBlocks<PREC, 0>::v)
+template <int PREC, bool MACRO, int BT>
+__global__ void __launch_bounds__(BT, MinBlocks<PREC, 0>::v * (kBatchBlock / BT))
 k_batch_step(const BatchArgs a)
 {
-    const int pb = a.blk_list[blockIdx.x];
-    const int s = a.blk_sample[pb];
+    using T = typename StoreOf<PREC>::T;
+    constexpr int H = kBatchBlock / BT; /* CTAs per pool block */
+    const int part = blockIdx.x % H;
+    const int pb = a.blk_list[blockIdx.x / H];
+    const int packed = a.blk_sample[pb];
+    const int s = packed >> 9;                  /* -1: free block */
+    const int k = part * BT + threadIdx.x;      /* node within the pool block */
+    const bool valid = s >= 0 && k < (packed & 511);
+    const long long i = (long long)pb * kBatchBlock + k;
+    /* L2 prefetch of the part of a pool block the CTA pf_blocks later steps */
+    if (a.pf_blocks > 0 && threadIdx.x == 0 && blockIdx.x + a.pf_blocks < gridDim.x) {
+        const unsigned c = blockIdx.x + a.pf_blocks;
+        prefetch_block<T>((const T *)a.fin, a.nbr, a.npad, a.npad,
+                          (long long)a.blk_list[c / H] * H + c % H, BT);
+    }
     double sum_u = 0.0, sum_r = 0.0;
     float dmax = 0.f;
+    /* the gathers first: they need only the node's place in the pool, so
+     * they are in flight while the sample record is staged */
+    T raw[Q];
+    if (valid) gather<T>((const T *)a.fin, a.nbr, a.npad, i, raw);
     /* the block's sample record, staged once in shared memory */
     __shared__ SampleDev sp;
     if (s >= 0) {
@@ -480,17 +508,16 @@ k_batch_step(const BatchArgs a)
         static_assert(sizeof(SampleDev) % 4 == 0, "SampleDev is copied as words");
         const uint32_t *src = (const uint32_t *)(a.samples + s);
         uint32_t *dst = (uint32_t *)&sp;
-        for (int k = threadIdx.x; k < words; k += kBatchBlock) dst[k] = src[k];
+        for (int w = threadIdx.x; w < words; w += BT) dst[w] = src[w];
     }
     __syncthreads();
-    if (s >= 0) {
-        const long long i = (long long)pb * kBatchBlock + threadIdx.x;
-        if (i - sp.base < sp.n) {
+    if (valid) {
+        {
             Coeffs co = sp.co;
             co.it = *a.t_base + a.t_off - sp.start;
             unsigned int fl = 0;
-            const Macro m = step_node<PREC, MACRO>(a.fin, a.fout, a.nbr, a.npad, i, co,
-                                                   fl, dmax);
+            const Macro m = collide_node<PREC, MACRO>(raw, (const T *)a.fin, (T *)a.fout,
+                                                      a.nbr, a.npad, i, co, fl, dmax);
             if (fl | (m.bad ? 4u : 0u)) atomicOr(a.serr + s, fl | (m.bad ? 4u : 0u));
             if (MACRO) {
                 const long long np = a.npad;
@@ -520,14 +547,15 @@ k_batch_step(const BatchArgs a)
         if (threadIdx.x == 0) {
             double tu = 0.0, tr = 0.0;
             float td = 0.f;
-            for (int k = 0; k < kBatchBlock / 32; k++) {
-                tu += su[k];
-                tr += sr[k];
-                td = fmaxf(td, sd[k]);
+            for (int w = 0; w < BT / 32; w++) {
+                tu += su[w];
+                tr += sr[w];
+                td = fmaxf(td, sd[w]);
             }
-            a.partial[pb] = tu;
-            a.partial[a.part_stride + pb] = tr;
-            a.partial[2 * a.part_stride + pb] = (double)td;
+            const long long row = (long long)pb * H + part;
+            a.partial[row] = tu;
+            a.partial[a.part_stride + row] = tr;
+            a.partial[2 * a.part_stride + row] = (double)td;
         }
     }
 }
@@ -591,13 +619,49 @@ int step_wave_blocks(int precision, int block, int variant)
     }
 }
 
+/* threads per CTA of the batch step: 128 for the fixed-point FP64 form
+ * (two CTAs per pool block; 4% faster in the plain kernel), 256 otherwise */
+template <int PREC> struct BatchCta { static constexpr int v = PREC == PLB_FP64 ? 128 : kBatchBlock; };
+
+int batch_ctas_per_block(int precision)
+{
+    return precision == PLB_FP64 ? kBatchBlock / BatchCta<PLB_FP64>::v : 1;
+}
+
+template <int PREC>
+static int batch_wave_prec()
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<PREC, false, BatchCta<PREC>::v>,
+                                                      BatchCta<PREC>::v, 0) != cudaSuccess)
+        return 0;
+    return sms * per;
+}
+
+int batch_wave_blocks(int precision)
+{
+    switch (precision) {
+    case PLB_FP64_EXACT: return batch_wave_prec<PLB_FP64_EXACT>();
+    case PLB_FP64: return batch_wave_prec<PLB_FP64>();
+    case PLB_FP64_FMA: return batch_wave_prec<PLB_FP64_FMA>();
+    case PLB_FP32: return batch_wave_prec<PLB_FP32>();
+    case PLB_FP16DEV: return batch_wave_prec<PLB_FP16DEV>();
+    case PLB_BF16DEV: return batch_wave_prec<PLB_BF16DEV>();
+    default: return 0;
+    }
+}
+
 template <int PREC>
 static cudaError_t launch_batch_prec(bool macros, const BatchArgs &a, int nb,
                                      cudaStream_t s)
 {
     if (nb == 0) return cudaSuccess;
-    if (macros) k_batch_step<PREC, true><<<nb, kBatchBlock, 0, s>>>(a);
-    else k_batch_step<PREC, false><<<nb, kBatchBlock, 0, s>>>(a);
+    constexpr int BT = BatchCta<PREC>::v;
+    const int grid = nb * (kBatchBlock / BT);
+    if (macros) k_batch_step<PREC, true, BT><<<grid, BT, 0, s>>>(a);
+    else k_batch_step<PREC, false, BT><<<grid, BT, 0, s>>>(a);
     return cudaGetLastError();
 }
 
