@@ -497,24 +497,18 @@ k_batch_step(const BatchArgs a)
     }
     double sum_u = 0.0, sum_r = 0.0;
     float dmax = 0.f;
-    /* the gathers first: they need only the node's place in the pool, so
-     * they are in flight while the sample record is staged */
+    /* the gathers first: they need only the node's place in the pool */
     T raw[Q];
     if (valid) gather<T>((const T *)a.fin, a.nbr, a.npad, i, raw);
-    /* the block's sample record, staged once in shared memory */
-    __shared__ SampleDev sp;
-    if (s >= 0) {
-        constexpr int words = (int)(sizeof(SampleDev) / 4);
-        static_assert(sizeof(SampleDev) % 4 == 0, "SampleDev is copied as words");
-        const uint32_t *src = (const uint32_t *)(a.samples + s);
-        uint32_t *dst = (uint32_t *)&sp;
-        for (int w = threadIdx.x; w < words; w += BT) dst[w] = src[w];
-    }
-    __syncthreads();
     if (valid) {
         {
-            Coeffs co = sp.co;
-            co.it = *a.t_base + a.t_off - sp.start;
+            /* the sample's coefficients straight from global memory (the
+             * same record for the whole CTA: cached after the first warp);
+             * no shared-memory staging, so no barrier makes the warps wait
+             * for each other's gathers */
+            const SampleDev *sp = a.samples + s;
+            Coeffs co = sp->co;
+            co.it = *a.t_base + a.t_off - sp->start;
             unsigned int fl = 0;
             const Macro m = collide_node<PREC, MACRO>(raw, (const T *)a.fin, (T *)a.fout,
                                                       a.nbr, a.npad, i, co, fl, dmax);
