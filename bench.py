@@ -426,6 +426,40 @@ def _steady_batch(samples, precision, K, max_steps, capacity=None):
     return out, node_steps, wall
 
 
+def run_pool(args):
+    """Throughput of the batch step on a fixed pool: --samples sphere packs of
+    --edge^3 (seeds 100, 101, ...; R ~ U[3, 6], porosity 0.35, tau 0.8,
+    F 5e-7) in the --precision form, stepped for --steps lattice steps in
+    intervals of --check-every (no sample retires), timed by wall clock
+    around the intervals after one warm-up interval."""
+    import torch
+    from porelb_gb300.batch import Batch
+    torch.cuda.set_device(0)
+    K = args.check_every
+    cap = int(args.samples * (args.edge ** 3 * 0.40 + 512))
+    b = Batch(cap, max(args.samples, 1), args.precision, check_every=K)
+    n = 0
+    for k in range(args.samples):
+        sid = b.add_packed(100 + k, args.edge, args.edge, args.edge, 3.0, 6.0, 0.35,
+                           0.8, 5e-7, tol=0.0, max_steps=10 ** 9)
+        n += b.num_nodes(sid)
+    b.run(1)
+    torch.cuda.synchronize()
+    intervals = max(1, args.steps // K)
+    t0 = time.perf_counter()
+    b.run(intervals)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    b.close()
+    line = {"metric": f"fluid MLUPS (batch step, {args.precision})",
+            "value": round(n * intervals * K / el / 1e6, 1), "unit": "MLUPS",
+            "steps": intervals * K, "num_node": n,
+            "config": {"workload": f"pool of {args.samples} sphere packs of "
+                                   f"{args.edge}^3, seeds 100+",
+                       "check_every": K, "precision": args.precision}}
+    print(json.dumps(line), flush=True)
+
+
 def run_batched(args):
     import torch
     import porelb_gb300 as P
@@ -627,7 +661,7 @@ def main():
                     help="seconds of CPU work in all for --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mode", default="plain",
-                    choices=["plain", "batched", "served", "precision"])
+                    choices=["plain", "batched", "served", "precision", "pool"])
     ap.add_argument("--samples", type=int, default=64)
     ap.add_argument("--check-every", type=int, default=1000)
     ap.add_argument("--max-steps", type=int, default=200000)
@@ -648,6 +682,8 @@ def main():
         return run_batched(args)
     if args.mode == "served":
         return run_served(args)
+    if args.mode == "pool":
+        return run_pool(args)
     if args.mode == "precision":
         return run_precision(args)
     args.warmup = max(args.warmup, 3)
