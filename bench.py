@@ -294,8 +294,10 @@ def run_gpu(args, rank, world, local):
     # End to end through the C ABI from host buffers, every call: the host
     # flag grid (preprocess's input) goes up, preprocess + alloc run on the
     # device (plb_create_from_flag), init, S lattice steps, and the macros
-    # come back.  The same through the V.bin table (plb_create from 152-byte
-    # records) is reported beside it.
+    # come back.  S defaults to 1000, the reference's interval between
+    # part-file dumps (porelb.c:436); the table is built again on every call.
+    # The same through the V.bin table (plb_create from 152-byte records) is
+    # reported beside it.
     e2e_steps = args.e2e_steps
 
     def pinned(a):
@@ -653,7 +655,9 @@ def main():
     ap.add_argument("--steady-wall", type=float, default=60.0,
                     help="seconds allowed for the untimed run to steady state "
                          "(0 = skip)")
-    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=1000,
+                    help="lattice steps per end-to-end call (default: the "
+                         "reference's interval between part-file dumps)")
     ap.add_argument("--e2e-reps", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=10.0,
                     help="seconds of the GPU arm's CPU-baseline sample")
