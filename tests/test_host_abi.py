@@ -174,3 +174,9 @@ def test_size_limits_rejected_before_any_device_work():
                               _lib.FP16DEV, 500, 0, 0,
                               ctypes.byref(h))
     assert rc == _lib.ERR_ARG
+
+
+def test_tuner_defaults_without_a_measurement():
+    from porelb_gb300 import tune
+    assert tune.best("fp32", 12345) == dict(block_size=0, ordering="morton",
+                                            kernel_variant=0)
