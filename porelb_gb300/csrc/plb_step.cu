@@ -474,8 +474,9 @@ k_step(const StepArgs a)
     }
 }
 
-/* Batch step: CTA b works on pool block blk_list[b], which belongs to sample
- * blk_sample[pool block]. */
+/* Batch step: kBatchBlock / BT CTAs of BT threads per active pool block;
+ * CTA b works on part b % H of pool block blk_list[b / H], whose map entry
+ * blk_sample[] packs its sample and that sample's node count in it. */
 template <int PREC, bool MACRO, int BT>
 __global__ void __launch_bounds__(BT, MinBlocks<PREC, 0>::v * (kBatchBlock / BT))
 k_batch_step(const BatchArgs a)
