@@ -51,7 +51,7 @@ __device__ __forceinline__ void gather(const T *fin, const uint32_t *nbr,
     f[0] = ldg_t(fin + i);
 #pragma unroll
     for (int j = 1; j < Q; j++) {
-        const int w = (int)__ldcs(nbr + (long long)(j - 1) * np + i);
+        const int w = (int)__ldg(nbr + (long long)(j - 1) * np + i);
         f[j] = ldg_t(fin + ((long long)j * np + w));
     }
 }
