@@ -7,7 +7,9 @@
  * porelb.c:318-365) and writes its 19 post-collision values to the other
  * ping-pong buffer.  Distributions are SoA, f[j][npad], so the 19 stores and
  * the 18 neighbour-word loads of a warp are fully coalesced; the gathers hit
- * nodes that the Morton order keeps close in memory.
+ * nodes that the Morton order keeps close in memory.  In the FP64 form each
+ * CTA also asks L2 for the node range of the block half a wave of resident
+ * blocks ahead (prefetch_block).
  *
  * Forms:
  *   FP64_EXACT  the reference's operations in the reference's order with
