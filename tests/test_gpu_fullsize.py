@@ -74,3 +74,19 @@ def test_c2_halfway_conserves_mass(c2):
         _, m1 = sim.reduce()
         assert abs(m1 - m0) <= 1e-12 * m0
         assert abs(m0 - sim.N) <= 1e-9 * sim.N
+
+
+def test_c2_fixed_point_within_1e12_of_exact_after_1000_steps(c2):
+    """The 256^3 workload for 1000 steps (the reference's first dump
+    interval): the fixed-point FP64 form stays within 1e-12 of the
+    bit-exact form on every distribution, and its permeability within
+    1e-10."""
+    out = []
+    for prec in ("fp64_exact", "fp64"):
+        with P.Simulation.from_flag(c2, *DIMS, tau=TAU, force=FORCE, precision=prec) as sim:
+            sim.init_dist_macro()
+            sim.step(1000)
+            out.append((sim.get_f(), sim.permeability()[0]))
+    (f_ex, k_ex), (f_fx, k_fx) = out
+    assert max_rel(f_fx, f_ex) <= 1e-12
+    assert abs(k_fx - k_ex) <= 1e-10 * abs(k_ex)
