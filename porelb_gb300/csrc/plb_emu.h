@@ -1,0 +1,71 @@
+/*
+ * plb_emu.h - IEEE-754 double multiply, round to nearest even, on the
+ * integer pipes.
+ *
+ * The bit-exact FP64 collision spends its time on GB300's FP64 pipe (about
+ * 2 operations per clock per SM).  Part of its multiplies run here instead,
+ * on the integer multiply-add pipe, and return the same bits as the FP64
+ * pipe: the 106-bit product of the two 53-bit significands is formed
+ * exactly and rounded once, to nearest, ties to even.  (An add done the same
+ * way cost the integer pipes more than it saved the FP64 pipe.)
+ *
+ * Domain: finite normal operands whose product is a normal number, or a
+ * zero operand (the result is then a zero of the product's sign).  The
+ * collision's values (distributions, densities, velocities, their squares
+ * and the run constants) all lie in it.
+ *
+ * Host+device, so a CPU build checks it against the host's multiply.
+ */
+#ifndef PLB_EMU_H_
+#define PLB_EMU_H_
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define EMU_HD __host__ __device__ __forceinline__
+#else
+#define EMU_HD static inline
+#endif
+
+namespace plb {
+namespace emu {
+
+constexpr uint64_t kM52 = 0xfffffffffffffull;
+constexpr uint64_t kH53 = 0x10000000000000ull;
+
+EMU_HD uint64_t umulhi(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+/* bits of a * b, both given as bits */
+EMU_HD uint64_t dmul_bits(uint64_t a, uint64_t b)
+{
+    const uint64_t sign = (a ^ b) & 0x8000000000000000ull;
+    const uint32_t ea = (uint32_t)(a >> 52) & 0x7ffu;
+    const uint32_t eb = (uint32_t)(b >> 52) & 0x7ffu;
+    if (ea == 0u || eb == 0u) return sign;
+    const uint64_t ma = (a & kM52) | kH53, mb = (b & kM52) | kH53;
+    const uint64_t hi = umulhi(ma, mb), lo = ma * mb; /* product in [2^104, 2^106) */
+    const uint32_t top = (uint32_t)(hi >> 41) & 1u;   /* bit 105 */
+    const uint32_t sh = 52u + top;
+    uint64_t m = (hi << (64u - sh)) | (lo >> sh);     /* [2^52, 2^53) */
+    const uint64_t rem = lo & ((1ull << sh) - 1ull);
+    const uint64_t half = 1ull << (sh - 1u);
+    m += (uint64_t)((rem > half) | ((rem == half) & (uint32_t)(m & 1u)));
+    uint32_t e = ea + eb - 1023u + top;
+    if (m >> 53) { /* rounded up to 2^53 */
+        m >>= 1;
+        e += 1u;
+    }
+    return sign | ((uint64_t)e << 52) | (m & kM52);
+}
+
+}  // namespace emu
+}  // namespace plb
+
+#endif
