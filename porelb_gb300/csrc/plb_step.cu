@@ -42,7 +42,7 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 /* the same product on the integer pipes (plb_emu.h): the same bits.  The
- * bit-exact collision sends 84 of its ~160 products per node here, which
+ * bit-exact collision sends 84 of its 97 products per node here, which
  * balances the FP64 and integer pipes (2.05 -> 2.68 GLUPS at 256^3). */
 __device__ __forceinline__ double imul(double a, double b)
 {
