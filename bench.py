@@ -26,6 +26,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "fluid MLUPS"
+DATA = "synthetic sphere pack (seeded splitmix64 generator)"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 
@@ -34,11 +35,50 @@ FALLBACK_HBM = 6800.0
 BYTES_PER_NODE = {"fp64_exact": 376, "fp64": 376, "fp64_fma": 376, "fp32": 224,
                   "fp16dev": 148, "bf16dev": 148}
 
-# DRAM bytes (read + write) of one launch of the step kernel without macros,
-# from a one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
-# of that launch in this script's own run, keyed by (workload, form, fluid
-# nodes): reported only for the workload that was captured
-NCU_TRAFFIC = {("c2_256", "fp64", 5871717): 1361580288 + 847561216}
+# DRAM bytes (read + write) of one step-kernel launch come from one-pass ncu
+# captures summarised in profiles/*.md, each with a line
+#   traffic-record: workload=W form=F num_node=N bytes=B source=D
+# where D is source_digest() of the step-kernel sources it was captured
+# from.  A record is reported only while the kernel sources are unchanged.
+PROFILES = os.path.join(ROOT, "profiles")
+STEP_SOURCES = ("plb_step.cu", "plb_fx.h", "plb_emu.h", "plb_internal.h")
+
+
+def source_digest():
+    import hashlib
+    h = hashlib.sha256()
+    for name in STEP_SOURCES:
+        with open(os.path.join(ROOT, "porelb_gb300", "csrc", name), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def recorded_traffic(workload, form, num_node):
+    """(bytes, profile file) of the matching capture, or (None, reason)."""
+    digest = source_digest()
+    stale = None
+    try:
+        names = sorted(os.listdir(PROFILES))
+    except OSError:
+        return None, "no profiles"
+    for name in names:
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(PROFILES, name)) as fh:
+            for line in fh:
+                if not line.startswith("traffic-record:"):
+                    continue
+                kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
+                if (kv.get("workload"), kv.get("form"), kv.get("num_node")) != \
+                        (workload, form, str(num_node)):
+                    continue
+                if kv.get("source") == digest:
+                    return int(kv["bytes"]), "profiles/" + name
+                stale = "profiles/" + name
+    if stale:
+        return None, f"{stale} was captured from other kernel sources"
+    return None, "no capture of this workload and form"
+
 
 WORKLOADS = {
     # plain FP64 at scale (the configuration the metric is quoted on)
@@ -138,6 +178,16 @@ def make_geometry(w):
     return flag, ns, phi
 
 
+def workload_config(name, w, num_node, phi, precision):
+    """The `config` object of both arms' JSON lines: the same keys and values
+    for the same workload."""
+    return {"workload": name, "dims": list(w["dims"]), "seed": w["seed"],
+            "radius": [w["rmin"], w["rmax"]], "porosity_target": w["porosity"],
+            "num_node": int(num_node), "porosity": phi, "tau": w["tau"],
+            "force": w["force"], "precision": precision,
+            "l2": "inputs larger than L2 (no flush)"}
+
+
 def cpu_port_mlups(V, vs, dims, w, budget_s, threads):
     """The oracle port (push-form reference algorithm, z-slab ranks as
     threads) on a bounded number of steps of the workload."""
@@ -171,20 +221,25 @@ def slab_count(nz, cores):
 
 
 def run_reference(args, rank, world):
+    """The reference algorithm on the host cores: the oracle port (push-form
+    stream and collision in the reference's operation order, z-slab ranks as
+    threads), on a table and geometry the oracle builds itself (its own
+    sphere-pack generator and build_V restatement), so that nothing of the
+    GPU library is loaded."""
     if rank != 0:
         return
-    import porelb_gb300 as P
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
     w = WORKLOADS[args.workload]
     dims = w["dims"]
-    flag, _, phi = make_geometry(w)
+    flag, _, phi = oracle_py.sphere_pack(w["seed"], *dims, w["rmin"], w["rmax"],
+                                         w["porosity"])
     cores = host_threads()
     p = slab_count(dims[2], cores)
-    V, vs = P.build_table(flag, *dims, p)
+    V, vs = oracle_py.build_v(flag, *dims, p)
     # one oracle solve for the whole run: W single warm-up steps, then K
     # bench steps of `per` lattice steps each, `per` sized so that the K
     # steps take about --ref-budget seconds in all
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_py
     s = oracle_py.OracleSim(V, *dims, vs, w["tau"], w["force"])
     s.init()
     it = 0
@@ -212,10 +267,9 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": round(value, 3),
         "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "dims": list(dims),
-                   "num_node": int(len(V)), "porosity": phi,
-                   "tau": w["tau"], "force": w["force"]},
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": workload_config(args.workload, w, len(V), phi, "fp64"),
+        "parallelism": f"{p} z-slab ranks on host threads",
         "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS",
                          "cores": p, "kind": "port",
                          "sample": f"{detail[0]} lattice step(s) of the full "
@@ -341,6 +395,7 @@ def run_gpu(args, rank, world, local):
         device=local, kernel_variant=kv))
 
     peak, peak_kind = hbm_peak()
+    traffic, traffic_src = recorded_traffic(args.workload, prec, N)
     bpn = BYTES_PER_NODE[prec]
     achieved = bpn * N / (ms_step * 1e-3) / 1e9
     line = {
@@ -349,28 +404,35 @@ def run_gpu(args, rank, world, local):
         "ms_per_step": round(ms_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec.startswith("fp64") else "f32",
-        "data": "synthetic sphere pack (seeded splitmix64 generator)",
-        "config": {"workload": args.workload, "dims": list(dims),
-                   "num_node": int(N), "porosity": phi, "tau": w["tau"],
-                   "force": w["force"], "precision": prec,
-                   "ordering": "morton",
-                   "l2": "inputs larger than L2 (no flush)",
-                   "parallelism": f"replicas{world}",
-                   "k_darcy_after_run": kd, "steady_state": steady},
+        "data": DATA,
+        "config": workload_config(args.workload, w, N, phi, prec),
+        "parallelism": f"replicas{world}",
+        "layout": "SoA f[19][npad] ping-pong, Morton node order",
+        "k_darcy_after_run": kd, "steady_state": steady,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
-                     "traffic": NCU_TRAFFIC.get((args.workload, prec, int(N))),
+                     "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "bytes_per_node": bpn, "peak_kind": peak_kind},
+        # one end-to-end call = upload, device build, init, e2e_steps lattice
+        # steps and the macros back; the per-step bytes are the call's bytes
+        # spread over its lattice steps
         "e2e": {"value": round(e2e, 3) if e2e else None, "unit": "MLUPS",
-                "h2d_bytes_per_step": int(fh.nbytes),
-                "d2h_bytes_per_step": int(rho.nbytes),
+                "h2d_bytes_per_step": round(fh.nbytes / e2e_steps, 1),
+                "d2h_bytes_per_step": round(rho.nbytes / e2e_steps, 1),
+                "h2d_bytes_per_call": int(fh.nbytes),
+                "d2h_bytes_per_call": int(rho.nbytes),
                 "lattice_steps_per_call": e2e_steps,
                 "host_memory": "pinned",
                 "path": "host flag grid -> plb_create_from_flag -> steps -> macros"},
         "e2e_vbin": {"value": round(e2e_v, 3) if e2e_v else None,
-                     "unit": "MLUPS", "h2d_bytes_per_step": int(Vh.nbytes),
-                     "d2h_bytes_per_step": int(rho.nbytes),
+                     "unit": "MLUPS",
+                     "h2d_bytes_per_step": round(Vh.nbytes / e2e_steps, 1),
+                     "d2h_bytes_per_step": round(rho.nbytes / e2e_steps, 1),
+                     "h2d_bytes_per_call": int(Vh.nbytes),
+                     "d2h_bytes_per_call": int(rho.nbytes),
+                     "lattice_steps_per_call": e2e_steps,
                      "path": "host V.bin table -> plb_create -> steps -> macros"},
         "gpu_launches": args.steps,
         "clocks": clk.result,

@@ -4,7 +4,7 @@
  * This is the drop-in boundary for porelb's hot path.  The reference has no
  * plugin or FFI layer: its "interface" is the SIMULATION* function set of one
  * C executable (porelb.h:127-165), the V.bin node table written by preprocess
- * (preprocess.c:211-238) and the part_%03d_%07d.bin macro dumps
+ * (preprocess.c:166-193) and the part_%03d_%07d.bin macro dumps
  * (porelb.c:375-391).  Each entry point below names the reference function or
  * file format it replaces.
  *
@@ -39,7 +39,7 @@ typedef struct {
 
 /* Fluid-node record, byte-compatible with NODE_INFO (porelb.h:73-76):
  * x@0 y@2 z@4, padding@6, nb_info[18]@8; 152 bytes.  nb_info[i] describes
- * the node at (x,y,z)+e[i+1], periodic (preprocess.c:183-196). */
+ * the node at (x,y,z)+e[i+1], periodic (preprocess.c:133-151). */
 typedef struct {
     uint16_t x, y, z;
     uint16_t pad_;
@@ -125,17 +125,17 @@ typedef struct plb_sim plb_sim;
  * porelb.c:83-94), FP64_EXACT, Morton order, automatic halo semantics. */
 void plb_default_params(plb_params *p);
 
-/* Replaces build_V (preprocess.c:74-209).  flag is nx*ny*nz uint8, x fastest,
+/* Replaces build_V (preprocess.c:29-164).  flag is nx*ny*nz uint8, x fastest,
  * 1 = fluid, 0 = solid.  With out == NULL only *num_node is computed.
  * v_sub_start receives num_p ints.  Requires nz % num_p == 0 (the reference
- * writes out of bounds otherwise, preprocess.c:152).  Fields that the
+ * writes out of bounds otherwise, preprocess.c:107).  Fields that the
  * reference leaves defined are reproduced bit-exactly; SOLID entries carry the
  * previous node's id/pid the way the reference's reused temporary does and
  * padding bytes are zero. */
 int plb_build_table(const uint8_t *flag, int nx, int ny, int nz, int num_p,
                     plb_node_info *out, int *num_node, int *v_sub_start);
 
-/* Replaces save_V (preprocess.c:211-238): header int32 num_node, num_p, nx,
+/* Replaces save_V (preprocess.c:166-193): header int32 num_node, num_p, nx,
  * ny, nz; int32 v_sub_start[num_p]; NODE_INFO[num_node]. */
 int plb_write_vbin(const char *path, const plb_node_info *V, int num_node,
                    int num_p, int nx, int ny, int nz, const int *v_sub_start);
@@ -173,7 +173,7 @@ int plb_create(const plb_node_info *V, int num_node, int nx, int ny, int nz,
 void plb_destroy(plb_sim *sim);
 
 /* build_V + plb_create in one device pass, from a flag grid (host buffer,
- * values 0/1, x fastest; num_p z slabs as preprocess.c:152).  No V.bin
+ * values 0/1, x fastest; num_p z slabs as preprocess.c:107).  No V.bin
  * records are formed: fluid cells are ranked in lexicographic order (the
  * reference node numbers) and along the Morton curve on the device.  The
  * handle is identical to plb_create on plb_build_table's output. */
@@ -232,6 +232,13 @@ int plb_permeability(plb_sim *sim, double *k_darcy, double *k_intrinsic);
 int plb_last_error(plb_sim *sim, int *it, int *node, int *x, int *y, int *z,
                    double *rho);
 
+/* What the step kernel reported since plb_init_equilibrium, read at each
+ * synchronising call: PLB_FLAG_FX_FALLBACK when the fixed-point FP64 form
+ * met a node whose populations left its range and recomputed that node in
+ * native FP64.  No reference counterpart (the reference has one form). */
+#define PLB_FLAG_FX_FALLBACK 2u
+int plb_kernel_flags(plb_sim *sim, unsigned *flags);
+
 /* Sizes and the handle's CUDA stream (a cudaStream_t). */
 int plb_info(plb_sim *sim, int *num_node, int *npad, int *precision,
              size_t *device_bytes);
@@ -285,6 +292,11 @@ int plb_batch_info(plb_batch *b, long long *t, int *active,
                    long long *used_nodes, long long *capacity_nodes,
                    size_t *device_bytes);
 int plb_batch_sample_nodes(plb_batch *b, int id, int *num_node);
+/* Room left in the pool, in nodes: the largest free block range (0 when no
+ * sample slot is free) and all free ranges together.  A sample of n fluid
+ * nodes can be admitted now when ceil(n / 256) * 256 <= *largest_range. */
+int plb_batch_free_nodes(plb_batch *b, long long *largest_range,
+                         long long *total);
 void *plb_batch_stream(plb_batch *b);
 
 /* ------------------------------------------------------- no allocation */
@@ -301,7 +313,11 @@ void *plb_batch_stream(plb_batch *b);
  * PLB_REDUCE_NOALLOC_MAX_NODES (larger n: PLB_ERR_ARG, nothing launched).
  * Calls share that array: calls that overlap on the GPU race.  The first
  * call on a device looks up the array's device address; make it before any
- * stream capture.  Asynchronous: out is valid once the stream reaches it. */
+ * stream capture.  That address is kept for the life of the process: it
+ * assumes the device's primary context is not reset while the library is
+ * in use (after cudaDeviceReset, or a primary-context reset through the
+ * driver API, the module may load at another address and later calls would
+ * use a stale one).  Asynchronous: out is valid once the stream reaches it. */
 #define PLB_REDUCE_NOALLOC_MAX_NODES 67108864LL
 int plb_reduce_noalloc(const double *ux, const double *rho, long long n,
                        double *out, void *stream);

@@ -72,6 +72,10 @@ def orc():
                                       _D, _I, _IP]
         lib.orc_reduce.argtypes = [_V, ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_double)]
+        lib.orc_sphere_pack.restype = _I
+        lib.orc_sphere_pack.argtypes = [ctypes.c_uint64, _I, _I, _I, _D, _D,
+                                        _D, _V, _IP,
+                                        ctypes.POINTER(ctypes.c_double)]
         _orc = lib
     return _orc
 
@@ -99,6 +103,20 @@ def _ref_libs():
 
 
 # ----------------------------------------------------------- restatement
+
+def sphere_pack(seed, nx, ny, nz, rmin, rmax, porosity):
+    """The synthetic geometry generator -> (flag, spheres, porosity); flag
+    is nx*ny*nz uint8, x fastest."""
+    lib = orc()
+    flag = np.empty(nx * ny * nz, np.uint8)
+    ns = ctypes.c_int()
+    phi = ctypes.c_double()
+    st = lib.orc_sphere_pack(seed, nx, ny, nz, rmin, rmax, porosity, _p(flag),
+                             ctypes.byref(ns), ctypes.byref(phi))
+    if st != 0:
+        raise ValueError(f"orc_sphere_pack status {st}")
+    return flag, ns.value, phi.value
+
 
 def build_v(flag, nx, ny, nz, num_p=1):
     lib = orc()

@@ -7,7 +7,7 @@
  *
  * It restates, in the reference's own operation order, the functions of the
  * hot path:
- *   build_V            preprocess.c:74-209
+ *   build_V            preprocess.c:29-164
  *   init_dist_macro    porelb.c:224-238
  *   stream_inner_nodes porelb.c:285-300
  *   update_recv_dist   porelb.c:302-312 (halo unpack after the local stream)
@@ -25,6 +25,7 @@
  */
 #include "porelb_oracle.h"
 
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -47,11 +48,11 @@ static const int OPP[Q] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9,
 
 /* ------------------------------------------------------------------ build_V */
 
-/* build_V (preprocess.c:74-209).  Fluid nodes are numbered in (z,y,x)
- * lexicographic order (preprocess.c:119-127); rank pid = z/(nz/num_p)
- * (preprocess.c:152); each node's record lands at v_sub_start[pid] +
- * position-within-rank (preprocess.c:199).  nb_info[i] describes the node at
- * x+e[i+1] with periodic wrap (preprocess.c:183-196): a zero flag makes it
+/* build_V (preprocess.c:29-164).  Fluid nodes are numbered in (z,y,x)
+ * lexicographic order (preprocess.c:74-82,99-113); rank pid = z/(nz/num_p)
+ * (preprocess.c:107); each node's record lands at v_sub_start[pid] +
+ * position-within-rank (preprocess.c:154).  nb_info[i] describes the node at
+ * x+e[i+1] with periodic wrap (preprocess.c:133-151): a zero flag makes it
  * SOLID and leaves id/pid as they were for the previous node (the reference
  * reuses one temporary record); any other flag value makes it FLUID (same
  * rank) or EXTERN with its position-within-rank and rank. */
@@ -483,4 +484,98 @@ int orc_pull_step(const uint8_t *kind, const uint32_t *src, int num_node,
     int b = collide_range(&tmp, it, 0, num_node);
     if (bad_node) *bad_node = b;
     return b >= 0 ? PLB_ERR_DENSITY : PLB_OK;
+}
+
+/* -------------------------------------------------------------- geometry */
+
+/* The synthetic geometry generator, restated from its definition (the
+ * reference reads flag.bin from outside and has no generator of its own):
+ * a splitmix64 stream (Steele, Lea & Flood, OOPSLA 2014) seeded with the
+ * configuration seed; each sphere draws its centre uniform in [0,n) per
+ * axis (x, y, z) and then its radius uniform in [rmin, rmax], each uniform
+ * from the top 53 bits of one draw; a cell is solid iff its periodic
+ * minimum-image squared distance to the centre, summed x then y then z, is
+ * at most r^2; spheres are added while the fluid fraction is above the
+ * target porosity.  Written independently of the library's generator so
+ * that the CPU baseline builds its input without the library; a CPU test
+ * checks the two give the same flag field byte for byte. */
+static uint64_t orc_mix(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static double orc_unit(uint64_t *s)
+{
+    return (double)(orc_mix(s) >> 11) / 9007199254740992.0; /* 2^53 */
+}
+
+/* the distinct cells of [c - r, c + r] on a periodic axis of n cells, each
+ * with its minimum-image distance to c; returns the count */
+static int orc_axis_cells(double c, double r, int n, int *cell, double *dist)
+{
+    long lo = (long)floor(c - r), hi = (long)ceil(c + r);
+    if (hi - lo + 1 > n) hi = lo + n - 1;
+    int m = 0;
+    for (long k = lo; k <= hi; k++) {
+        const int idx = (int)(((k % n) + n) % n);
+        double d = fabs((double)idx - c);
+        if ((double)n - d < d) d = (double)n - d;
+        cell[m] = idx;
+        dist[m] = d;
+        m++;
+    }
+    return m;
+}
+
+int orc_sphere_pack(uint64_t seed, int nx, int ny, int nz, double rmin,
+                    double rmax, double porosity, uint8_t *flag,
+                    int *num_spheres, double *porosity_out)
+{
+    if (!flag || nx <= 0 || ny <= 0 || nz <= 0 || !(rmin > 0.0) ||
+        rmax < rmin || !(porosity >= 0.0) || !(porosity <= 1.0))
+        return PLB_ERR_ARG;
+    const size_t cells = (size_t)nx * ny * nz;
+    for (size_t k = 0; k < cells; k++) flag[k] = 1;
+    int nmax = nx > ny ? nx : ny;
+    if (nz > nmax) nmax = nz;
+    int *cx = malloc(sizeof(int) * (size_t)nmax * 3);
+    double *dx = malloc(sizeof(double) * (size_t)nmax * 3);
+    if (!cx || !dx) {
+        free(cx);
+        free(dx);
+        return PLB_ERR_NOMEM;
+    }
+    int *cy = cx + nmax, *cz = cx + 2 * nmax;
+    double *dy = dx + nmax, *dz = dx + 2 * nmax;
+    uint64_t st = seed;
+    size_t solid = 0;
+    int count = 0;
+    while ((double)(cells - solid) / (double)cells > porosity && count < 100000000) {
+        const double px = orc_unit(&st) * nx;
+        const double py = orc_unit(&st) * ny;
+        const double pz = orc_unit(&st) * nz;
+        const double r = rmin + (rmax - rmin) * orc_unit(&st);
+        count++;
+        const int mx = orc_axis_cells(px, r, nx, cx, dx);
+        const int my = orc_axis_cells(py, r, ny, cy, dy);
+        const int mz = orc_axis_cells(pz, r, nz, cz, dz);
+        for (int c = 0; c < mz; c++)
+            for (int b = 0; b < my; b++) {
+                uint8_t *row = flag + ((size_t)cz[c] * ny + cy[b]) * nx;
+                for (int a = 0; a < mx; a++) {
+                    const double d2 = dx[a] * dx[a] + dy[b] * dy[b] + dz[c] * dz[c];
+                    if (!(d2 <= r * r) || !row[cx[a]]) continue;
+                    row[cx[a]] = 0;
+                    solid++;
+                }
+            }
+    }
+    free(cx);
+    free(dx);
+    if (num_spheres) *num_spheres = count;
+    if (porosity_out) *porosity_out = (double)(cells - solid) / (double)cells;
+    return PLB_OK;
 }

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-/* build_V restated (preprocess.c:74-209).  See the C file for details. */
+/* build_V restated (preprocess.c:29-164).  See the C file for details. */
 int orc_build_v(const uint8_t *flag, int nx, int ny, int nz, int num_p,
                 plb_node_info *out, int *num_node, int *v_sub_start);
 
@@ -67,6 +67,14 @@ int orc_pull_step(const uint8_t *kind, const uint32_t *src, int num_node,
                   double *f0, double *f1, double *rho, double *ux, double *uy,
                   double *uz, double tau, double force_x, int it,
                   int *bad_node);
+
+/* The synthetic sphere-pack generator (splitmix64, periodic minimum image,
+ * spheres added until the porosity reaches the target): flag is nx*ny*nz
+ * bytes, x fastest, 1 fluid / 0 solid.  The same field as the library's
+ * plb_sphere_pack, written independently. */
+int orc_sphere_pack(uint64_t seed, int nx, int ny, int nz, double rmin,
+                    double rmax, double porosity, uint8_t *flag,
+                    int *num_spheres, double *porosity_out);
 
 /* Sum of Ux and Rho in node order (FP64, serial). */
 void orc_reduce(orc_sim *s, double *sum_ux, double *mass);

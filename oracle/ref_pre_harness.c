@@ -10,7 +10,7 @@
 #include "preprocess.c"
 #undef main
 
-/* Runs build_V (preprocess.c:74-209) on flag_path and copies the result.
+/* Runs build_V (preprocess.c:29-164) on flag_path and copies the result.
  * out receives num_node NODE_INFO records (may be NULL to query the count);
  * v_sub_start receives num_p ints.  Returns num_node. */
 int ref_build_v(const char *flag_path, int nx, int ny, int nz, int num_p,
@@ -24,7 +24,7 @@ int ref_build_v(const char *flag_path, int nx, int ny, int nz, int num_p,
     return n;
 }
 
-/* Runs save_V (preprocess.c:211-238) on a table built by build_V. */
+/* Runs save_V (preprocess.c:166-193) on a table built by build_V. */
 int ref_build_and_save_v(const char *flag_path, int nx, int ny, int nz,
                          int num_p, const char *vbin_path)
 {

@@ -108,7 +108,10 @@ _SIGS = {
                             ctypes.POINTER(ctypes.c_longlong),
                             ctypes.POINTER(ctypes.c_longlong),
                             ctypes.POINTER(ctypes.c_size_t)]),
+    "plb_kernel_flags": (_I, [_P, ctypes.POINTER(ctypes.c_uint)]),
     "plb_batch_sample_nodes": (_I, [_P, _I, _IP]),
+    "plb_batch_free_nodes": (_I, [_P, ctypes.POINTER(ctypes.c_longlong),
+                                  ctypes.POINTER(ctypes.c_longlong)]),
     "plb_batch_stream": (_P, [_P]),
     "plb_reduce_noalloc": (_I, [_P, _P, ctypes.c_longlong, _P, _P]),
 }

@@ -51,7 +51,7 @@ def _iptr(a):
 # ------------------------------------------------------------------ tables
 
 def build_table(flag, nx, ny, nz, num_p=1):
-    """preprocess's build_V (preprocess.c:74-209) -> (V, v_sub_start)."""
+    """preprocess's build_V (preprocess.c:29-164) -> (V, v_sub_start)."""
     lib = _lib.load()
     flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
     if flag.size != nx * ny * nz:
@@ -73,7 +73,7 @@ def check_table(V, nx, ny, nz, v_sub_start):
 
 
 def write_vbin(path, V, v_sub_start, nx, ny, nz):
-    """preprocess's save_V (preprocess.c:211-238)."""
+    """preprocess's save_V (preprocess.c:166-193)."""
     lib = _lib.load()
     vs = np.ascontiguousarray(v_sub_start, dtype=np.int32)
     V = np.ascontiguousarray(V, dtype=NODE_DTYPE)
@@ -241,6 +241,13 @@ class Simulation:
             return None
         return dict(it=v[0].value, node=v[1].value, x=v[2].value,
                     y=v[3].value, z=v[4].value, rho=r.value)
+
+    def kernel_flags(self):
+        """PLB_FLAG_* bits the step kernel reported since init (2: nodes
+        recomputed in native FP64 by the fixed-point form)."""
+        f = ctypes.c_uint(0)
+        _check(self._lib.plb_kernel_flags(self._h, ctypes.byref(f)), "kernel_flags")
+        return f.value
 
     def info(self):
         n, npad, prec = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -120,6 +120,14 @@ class Batch:
                                               _ptr(out[3])), "get_macros")
         return out
 
+    def free_nodes(self):
+        """(largest free block range, all free ranges) in nodes; the largest
+        range is 0 when no sample slot is free."""
+        big, tot = ctypes.c_longlong(), ctypes.c_longlong()
+        _check(self._lib.plb_batch_free_nodes(self._h, ctypes.byref(big),
+                                              ctypes.byref(tot)), "free_nodes")
+        return big.value, tot.value
+
     def info(self):
         t, used, cap = (ctypes.c_longlong() for _ in range(3))
         act = ctypes.c_int()

@@ -762,6 +762,21 @@ int plb_batch_info(plb_batch *b, long long *t, int *active, long long *used_node
     return PLB_OK;
 }
 
+int plb_batch_free_nodes(plb_batch *b, long long *largest_range, long long *total)
+{
+    if (!b) return PLB_ERR_ARG;
+    long long big = 0, all = 0;
+    for (const auto &r : b->free_blocks) {
+        big = std::max(big, r.second);
+        all += r.second;
+    }
+    int slots = 0;
+    for (const auto &h : b->s) slots += !h.used;
+    if (largest_range) *largest_range = slots > 0 ? big * B : 0;
+    if (total) *total = all * B;
+    return PLB_OK;
+}
+
 int plb_batch_sample_nodes(plb_batch *b, int id, int *num_node)
 {
     if (!b || id < 0 || id >= b->max_samples || !b->s[id].used || !num_node)

@@ -9,10 +9,14 @@
  * exactly and rounded once, to nearest, ties to even.  (An add done the same
  * way cost the integer pipes more than it saved the FP64 pipe.)
  *
- * Domain: finite normal operands whose product is a normal number, or a
- * zero operand (the result is then a zero of the product's sign).  The
- * collision's values (distributions, densities, velocities, their squares
- * and the run constants) all lie in it.
+ * Domain of the integer path: finite normal operands whose product is a
+ * normal number, or a zero times a finite operand (a zero of the product's
+ * sign).  The collision's values (distributions, densities, velocities,
+ * their squares and the run constants) all lie in it.  Everything else (an
+ * infinite or NaN operand, a subnormal operand, a product that could
+ * overflow or fall below the normal range) takes the native multiply, so
+ * the bits are the IEEE product's everywhere and a diverging run carries
+ * its infinities and NaNs forward.
  *
  * Host+device, so a CPU build checks it against the host's multiply.
  */
@@ -42,13 +46,38 @@ EMU_HD uint64_t umulhi(uint64_t a, uint64_t b)
 #endif
 }
 
+/* the native product, bits in and out */
+EMU_HD uint64_t dmul_native(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(
+        __dmul_rn(__longlong_as_double((long long)a), __longlong_as_double((long long)b)));
+#else
+    double x, y;
+    __builtin_memcpy(&x, &a, 8);
+    __builtin_memcpy(&y, &b, 8);
+    volatile double p = x * y;
+    double q = p;
+    uint64_t r;
+    __builtin_memcpy(&r, &q, 8);
+    return r;
+#endif
+}
+
 /* bits of a * b, both given as bits */
 EMU_HD uint64_t dmul_bits(uint64_t a, uint64_t b)
 {
     const uint64_t sign = (a ^ b) & 0x8000000000000000ull;
     const uint32_t ea = (uint32_t)(a >> 52) & 0x7ffu;
     const uint32_t eb = (uint32_t)(b >> 52) & 0x7ffu;
-    if (ea == 0u || eb == 0u) return sign;
+    /* a zero times a finite value */
+    if (((a << 1) == 0ull && eb != 0x7ffu) || ((b << 1) == 0ull && ea != 0x7ffu))
+        return sign;
+    /* normal operands with a normal product: 1 <= ea, eb <= 2046 and the
+     * biased result exponent ea + eb - 1023 (+1 for a significand product
+     * >= 2, +1 more for a rounding carry) within [1, 2046] */
+    if (ea - 1u >= 2046u || eb - 1u >= 2046u || ea + eb - 1024u > 2043u)
+        return dmul_native(a, b);
     const uint64_t ma = (a & kM52) | kH53, mb = (b & kM52) | kH53;
     const uint64_t hi = umulhi(ma, mb), lo = ma * mb; /* product in [2^104, 2^106) */
     const uint32_t top = (uint32_t)(hi >> 41) & 1u;   /* bit 105 */

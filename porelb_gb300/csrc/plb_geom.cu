@@ -2,7 +2,7 @@
  * plb_geom.cu - device-side geometry: the periodic sphere-pack generator and
  * the node table built straight from a flag grid.
  *
- * build_V (preprocess.c:74-209) numbers fluid cells (flag == 1) in x-fastest
+ * build_V (preprocess.c:29-164) numbers fluid cells (flag == 1) in x-fastest
  * lexicographic order and stores, per node, the 18 neighbours at x + e_j.
  * From a flag grid the same information is a bit test: here the fluid cells
  * are ranked twice with popcount scans over bitmaps - once in lexicographic

@@ -52,7 +52,7 @@ const char *plb_status_string(int s)
 
 /* ------------------------------------------------------------ node table */
 
-/* The table follows build_V (preprocess.c:74-209): fluid nodes (flag == 1)
+/* The table follows build_V (preprocess.c:29-164): fluid nodes (flag == 1)
  * numbered in x-fastest lexicographic order, rank = z / (nz/num_p), each
  * record placed at v_sub_start[rank] + its position within the rank.
  * Neighbour slot d describes (x,y,z)+e[d+1] with periodic wrap.  A zero flag

@@ -94,7 +94,10 @@ __global__ void k_final(const double *part, long long nb, double *out)
 
 /* The device address of g_partials on the current device.  In host code
  * g_partials names a host-side stand-in, not device memory, so the address
- * is looked up once per device with that device current and kept. */
+ * is looked up once per device with that device current and kept.  The
+ * cache is keyed by device ordinal and assumes the device's primary context
+ * outlives the library's use: a context reset (cudaDeviceReset) may reload
+ * the module at another address, which this cache would not see. */
 static int partials_on_current_device(double **addr)
 {
     int dev = -1;

@@ -887,6 +887,7 @@ int plb_init_equilibrium(plb_sim *s)
     CK(cudaStreamSynchronize(s->stream));
     s->cur = 0;
     s->initialized = 1;
+    s->fallback_nodes_seen = 0;
     s->macro_valid = 1;
     s->err_it = -1;
     s->err_node = -1;
@@ -1123,6 +1124,13 @@ int plb_last_error(plb_sim *s, int *it, int *node, int *x, int *y, int *z,
         if (z) *z = c[2];
     }
     return PLB_ERR_DENSITY;
+}
+
+int plb_kernel_flags(plb_sim *s, unsigned *flags)
+{
+    if (!s || !flags) return PLB_ERR_ARG;
+    *flags = s->fallback_nodes_seen ? PLB_FLAG_FX_FALLBACK : 0u;
+    return PLB_OK;
 }
 
 int plb_info(plb_sim *s, int *num_node, int *npad, int *precision,

@@ -1,6 +1,6 @@
 /*
  * preprocess_main.c - drop-in replacement of the reference preprocess
- * executable (preprocess.c:240-249, "preprocess.x np").
+ * executable (preprocess.c:195-204, "preprocess.x np").
  *
  * Reads flag.bin (uint8 [z][y][x], 1 fluid, 0 solid) and writes V.bin.  The
  * reference hard-codes a 400^3 grid and both file names; they are the

@@ -4,13 +4,13 @@ getK.c (getK.c:39-95) estimates the permeability of a BCC array of spheres
 of radius a = sqrt(3) L chi / 4 (chi in (0, 1]; chi = 1 when neighbours
 touch) with L = nx - 1:
 
-* K1 (getK.c:66-70): Stokes drag of the array, K = 2/9 a^2 / (d* (1 - eps)),
+* K1 (getK.c:67-70): Stokes drag of the array, K = 2/9 a^2 / (d* (1 - eps)),
   with d*(chi) = sum_i q_i chi^i the drag-coefficient series of Sangani &
   Acrivos (1982) for BCC arrays (31 coefficients, getK.c:5-36).
-* K2 (getK.c:62-72): Kozeny-Carman, eps^3 / (C S^2), C = 5,
+* K2 (getK.c:61-64,72): Kozeny-Carman, eps^3 / (C S^2), C = 5,
   S = 2 * 4 pi a^2 / L^3.
 eps = 1 - 8/3 pi a^3 / L^3 is the porosity of two spheres per cell.
-The TABLE build (getK.c:86-99) multiplies K1 by eps.
+The TABLE build (getK.c:74-92) multiplies K1 by eps.
 
 These are the reference's validation numbers for the half-way bounce-back
 mode: they are not computed from simulation output.

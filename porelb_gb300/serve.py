@@ -25,15 +25,36 @@ import numpy as np
 from .batch import Batch
 
 
+# a request whose estimated fluid nodes exceed the free room by more than
+# this factor is not tried: the generator stops at or just below the target
+# porosity, so edge^3 * porosity over-estimates its nodes by a few percent
+_EST_SLACK = 0.9
+
+BLOCK = 256  # pool block (nodes)
+
+
+def _blocks_nodes(n):
+    return -(-int(n) // BLOCK) * BLOCK
+
+
 class Server:
     def __init__(self, hbm_budget_bytes, precision="fp32", check_every=500,
-                 max_samples=4096, device=0, lookahead=64):
-        bpn = Batch.bytes_per_node(precision)
-        self.capacity = int(hbm_budget_bytes // bpn)
-        self.batch = Batch(self.capacity, max_samples, precision, check_every,
-                           device=device)
+                 max_samples=4096, device=0, lookahead=64, batch=None):
+        if batch is None:
+            bpn = Batch.bytes_per_node(precision)
+            self.capacity = int(hbm_budget_bytes // bpn)
+            batch = Batch(self.capacity, max_samples, precision, check_every,
+                          device=device)
+        self.batch = batch
+        self.capacity = int(batch.info()["capacity_nodes"])
         self.precision = precision
         self.lookahead = lookahead
+
+    @staticmethod
+    def estimated_nodes(r):
+        """Fluid nodes a request will have, estimated before its geometry is
+        built (edge^3 * porosity)."""
+        return r.edge ** 3 * r.porosity
 
     def close(self):
         self.batch.close()
@@ -46,6 +67,7 @@ class Server:
         waiting = []
         live = {}
         done = []
+        rejected = []
         t0 = time.perf_counter()
         node_steps = 0
         intervals = 0
@@ -61,7 +83,16 @@ class Server:
             # not fit into the free node ranges
             admitted = []
             ta = time.perf_counter()
+            room = self.batch.free_nodes()[0]
             for r in waiting[: self.lookahead]:
+                est = _EST_SLACK * self.estimated_nodes(r)
+                if est > self.capacity:
+                    # larger than the whole pool: it can never be admitted
+                    rejected.append(self._reject(r, t0, time_scale))
+                    admitted.append(r)
+                    continue
+                if live and _blocks_nodes(est) > room:
+                    continue  # no room now: skip building its geometry
                 sid = self.batch.try_add_packed(
                     r.seed, r.edge, r.edge, r.edge, r.rmin, r.rmax, r.porosity,
                     r.tau, r.force, tol=r.tol)
@@ -69,6 +100,13 @@ class Server:
                     live[sid] = dict(req=r, admitted=time.perf_counter() - t0,
                                      nodes=self.batch.num_nodes(sid))
                     admitted.append(r)
+                    room = self.batch.free_nodes()[0]
+                elif not live:
+                    # it did not fit into the empty pool: it never will
+                    rejected.append(self._reject(r, t0, time_scale))
+                    admitted.append(r)
+                else:
+                    room = self.batch.free_nodes()[0]
             for r in admitted:
                 waiting.remove(r)
             t_admit += time.perf_counter() - ta
@@ -103,5 +141,14 @@ class Server:
                        fluid_mlups=node_steps / wall / 1e6 if wall > 0 else 0.0,
                        intervals=intervals, capacity_nodes=self.capacity,
                        admit_s=t_admit, run_s=t_run,
-                       precision=self.precision, check_every=K)
+                       precision=self.precision, check_every=K,
+                       rejected=[d["index"] for d in rejected])
         return done, summary
+
+    @staticmethod
+    def _reject(r, t0, time_scale):
+        """Record of a request that cannot fit into the pool even when the
+        pool is empty (status PLB_ERR_NOMEM)."""
+        return dict(index=r.index, edge=r.edge, status=-5,
+                    arrival=r.arrival * time_scale,
+                    finished=time.perf_counter() - t0)

@@ -41,5 +41,23 @@ extern "C" long emu_check(long n, unsigned long long seed)
     const double z[] = {0.0, -0.0, 1.0, -1.0, 1.0 / 3};
     for (double p : z)
         for (double q : z) check(p, q);
+    /* outside the integer path: infinities, NaNs, subnormals, products that
+     * overflow or underflow, and the edges of the normal range */
+    const double sp[] = {INFINITY, -INFINITY, NAN, -NAN, 0.0, -0.0, 1.0, -2.5,
+                         ldexp(1.0, -1074), ldexp(-3.0, -1060), ldexp(1.0, -1022),
+                         ldexp(1.5, -1022), ldexp(1.0, 1023), ldexp(-1.9, 1023),
+                         ldexp(1.0, 512), ldexp(1.0, -512), ldexp(1.7, 511),
+                         ldexp(1.3, -511), 1e-300, -1e300, 1.0 / 3};
+    for (double p : sp)
+        for (double q : sp) check(p, q);
+    for (long k = 0; k < n / 10; k++) {
+        /* exponents spread over the whole range, both signs */
+        const int xa = (int)(g() % 2200) - 1100, xb = (int)(g() % 2200) - 1100;
+        check(U(g) * ldexp(1.0, xa), U(g) * ldexp(1.0, xb));
+        /* products at the edges of the normal range */
+        const int t = (int)(g() % 8);
+        check(U(g) * ldexp(1.0, -511 - t), U(g) * ldexp(1.0, -511 + (int)(g() % 8)));
+        check(U(g) * ldexp(1.0, 511 + t), U(g) * ldexp(1.0, 512 - (int)(g() % 8)));
+    }
     return bad;
 }

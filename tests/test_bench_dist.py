@@ -76,3 +76,32 @@ def test_reference_arm_line_on_rank0(monkeypatch, capsys):
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert took < 60
+
+
+def test_reference_arm_loads_no_library_code():
+    """The reference arm builds its geometry and table with the oracle and
+    runs the oracle port: the GPU library is neither imported nor mapped,
+    and its config equals the GPU arm's for the same workload."""
+    import json
+    import subprocess
+    code = (
+        "import sys, json; sys.argv = ['bench.py', '--impl', 'reference', "
+        "'--workload', 'c1_64', '--steps', '3', '--warmup', '3', '--ref-budget', '1'];"
+        "import bench; bench.main();"
+        "maps = open('/proc/self/maps').read();"
+        "print(json.dumps({'lib_mapped': 'libporelb_gpu' in maps, "
+        "'pkg': 'porelb_gb300' in sys.modules}))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True,
+                         text=True, timeout=300, env=dict(os.environ, RANK="0",
+                                                          WORLD_SIZE="1"))
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(x) for x in out.stdout.strip().splitlines() if x.startswith("{")]
+    probe, line = lines[-1], lines[-2]
+    assert probe == {"lib_mapped": False, "pkg": False}
+    sys.path.insert(0, ROOT)
+    import bench
+    import porelb_gb300 as P
+    w = bench.WORKLOADS["c1_64"]
+    flag, _, phi = P.sphere_pack(w["seed"], *w["dims"], w["rmin"], w["rmax"], w["porosity"])
+    V, _ = P.build_table(flag, *w["dims"], 1)
+    assert line["config"] == bench.workload_config("c1_64", w, len(V), phi, "fp64")

@@ -10,7 +10,22 @@ import pytest
 
 from porelb_gb300 import getk
 
-REF = "/root/reference/getK.c"
+
+
+def _ref_dir():
+    """The reference tree: $REF_DIR, else the one oracle/Makefile built
+    oracle/_ref from (recorded in oracle/_ref/REF_DIR); '' when neither."""
+    d = os.environ.get("REF_DIR", "")
+    if not d:
+        rec = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "oracle", "_ref", "REF_DIR")
+        if os.path.exists(rec):
+            with open(rec) as fh:
+                d = fh.read().strip()
+    return d
+
+
+REF = os.path.join(_ref_dir(), "getK.c") if _ref_dir() else ""
 
 
 def test_series_and_porosity():
@@ -21,7 +36,7 @@ def test_series_and_porosity():
     assert len(getk.QS_BCC) == 31 and getk.QS_BCC[0] == 1.0
 
 
-@pytest.mark.skipif(not os.path.exists(REF), reason="reference tree not present")
+@pytest.mark.skipif(not REF or not os.path.exists(REF), reason="reference tree not present")
 @pytest.mark.parametrize("chi,nx", [("0.3", "64"), ("0.6", "128"), ("0.95", "33")])
 def test_getk_matches_reference_program(tmp_path, chi, nx):
     src = open(REF).read()

@@ -90,3 +90,29 @@ def test_c2_fixed_point_within_1e12_of_exact_after_1000_steps(c2):
     (f_ex, k_ex), (f_fx, k_fx) = out
     assert max_rel(f_fx, f_ex) <= 1e-12
     assert abs(k_fx - k_ex) <= 1e-10 * abs(k_ex)
+
+
+def test_c2_fixed_point_steady_state_permeability_within_1e10_of_exact(c2):
+    """The 256^3 workload run to its steady state (relative change of <u_x>
+    below 1e-7 over 1000 steps, about 3000 steps, the state whose
+    permeability the bench reports): the fixed-point FP64 form's permeability
+    within 1e-10 of the bit-exact form's at the same step, and the same
+    convergence step."""
+    ks = {}
+    for prec in ("fp64_exact", "fp64"):
+        with P.Simulation.from_flag(c2, *DIMS, tau=TAU, force=FORCE, precision=prec) as sim:
+            sim.init_dist_macro()
+            it, prev, hist = 0, None, []
+            while it < 10000:
+                sim.step(1000, it_begin=it)
+                it += 1000
+                k = sim.permeability()[0]
+                hist.append(k)
+                if prev is not None and abs(k - prev) <= 1e-7 * abs(k):
+                    break
+                prev = k
+            ks[prec] = (it, hist)
+    (it_ex, h_ex), (it_fx, h_fx) = ks["fp64_exact"], ks["fp64"]
+    assert it_ex == it_fx and it_ex < 10000
+    for a, b in zip(h_fx, h_ex):
+        assert abs(a - b) <= 1e-10 * abs(b), f"k {a!r} vs exact {b!r}"

@@ -156,6 +156,60 @@ def test_fp64_fixed_point_within_1e12_high_velocity(case):
         assert max_rel(sim.macros()[0], s.macros()[0]) <= 1e-12
 
 
+def oracle_pull_from(V, vs, f0, tau, force, it_begin, steps):
+    """The oracle's pull-form restatement stepped from the state f0 (AoS,
+    reference order); slots no push or bounce writes keep w_j, as the
+    reference's f1 does from its initialisation (porelb.c:224-238)."""
+    import ctypes
+    lib = O.orc()
+    kind, src = O.pull_table(V, vs)
+    N = len(V)
+    f0 = np.ascontiguousarray(f0, dtype=np.float64).copy()
+    f1 = np.tile(np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12), N)
+    mac = np.zeros((4, N))
+    bad = ctypes.c_int()
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    for it in range(it_begin, it_begin + steps):
+        assert lib.orc_pull_step(p(kind), p(src), N, p(f0), p(f1), p(mac[0]), p(mac[1]),
+                                 p(mac[2]), p(mac[3]), tau, force, it,
+                                 ctypes.byref(bad)) == 0
+    return f0, mac
+
+
+def test_fixed_point_fallback_fires_and_stays_within_1e12():
+    """A state whose populations lie far outside the fixed-point form's range
+    (deviations up to 60% of the weights at one node in twenty): those
+    nodes are recomputed in native FP64, the kernel reports it, and the
+    result stays within 1e-12 of the oracle; the bit-exact form equals it."""
+    dims, tau, force, steps = (20, 18, 16), 0.8, 1e-4, 3
+    flag = pack_flag(dims, 9, 2.5, 4.0, 0.45)
+    V, vs = P.build_table(flag, *dims, 1)
+    N = len(V)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    rng = np.random.default_rng(5)
+    f = np.tile(w, (N, 1)) * (1 + 0.05 * rng.uniform(-1, 1, (N, 19)))
+    hit = rng.random(N) < 0.05
+    f[hit] = w * (1 + 0.6 * rng.uniform(-1, 1, (int(hit.sum()), 19)))
+    f /= f.sum(axis=1, keepdims=True)  # density 1 at every node
+    dev = np.abs(f / w - 1)
+    assert (dev[hit] > 0.45).any(axis=1).mean() > 0.9
+    ref_f, ref_mac = oracle_pull_from(V, vs, f.reshape(-1), tau, force, 1, steps)
+    for prec in ("fp64", "fp64_exact"):
+        with gpu_run(V, dims, vs, tau, force, 0, precision=prec) as sim:
+            sim.set_f(f.reshape(-1))
+            sim.step(steps, it_begin=1)
+            got = sim.get_f()
+            if prec == "fp64":
+                assert sim.kernel_flags() & 2, "the native-FP64 fallback did not fire"
+                assert max_rel(got, ref_f) <= 1e-12
+                assert max_rel(sim.macros()[0], ref_mac[0]) <= 1e-12
+            else:
+                assert (got == ref_f).all()
+    # a state inside the range does not fire it
+    with gpu_run(V, dims, vs, tau, force, 40, precision="fp64") as sim:
+        assert sim.kernel_flags() == 0
+
+
 @pytest.mark.parametrize("dims", [(96, 96, 96), (12, 10, 9)])
 def test_fp64_kernel_variants_agree_bitwise(dims):
     """Every FP64 step kernel (128-, 80- and 64-register, with and without

@@ -73,7 +73,7 @@ def test_read_vbin_errors(tmp_path):
 
 
 def test_build_table_rejects_uneven_slabs():
-    # the reference writes out of bounds when nz % num_p != 0 (preprocess.c:152)
+    # the reference writes out of bounds when nz % num_p != 0 (preprocess.c:107)
     flag = np.ones(4 * 4 * 6, np.uint8)
     with pytest.raises(P.PorelbError) as e:
         P.build_table(flag, 4, 4, 6, num_p=4)

@@ -167,3 +167,19 @@ def test_live_reference_dump_schedule(tmp_path):
     s.run(1)
     got = np.fromfile(tmp_path / "part_000_0000000.bin", np.float64).reshape(4, -1)
     assert (got == s.macros()).all()
+
+
+@pytest.mark.parametrize("case", [
+    (0, 64, 64, 64, 6.0, 6.0, 0.40),      # the 64^3 plain configuration
+    (1, 256, 256, 256, 4.0, 10.0, 0.35),  # the 256^3 plain FP64 workload
+    (7, 20, 9, 13, 3.0, 11.0, 0.30),      # spheres wider than the box
+])
+def test_oracle_sphere_pack_equals_library(case):
+    """The oracle's own generator (which the CPU baseline builds its input
+    with) gives the library's flag field byte for byte."""
+    seed, nx, ny, nz, rmin, rmax, phi = case
+    fo, no, po = O.sphere_pack(seed, nx, ny, nz, rmin, rmax, phi)
+    fp, npk, pp = P.sphere_pack(seed, nx, ny, nz, rmin, rmax, phi)
+    assert no == npk and po == pp
+    assert np.array_equal(fo, fp)
+    assert po <= phi and 0 < fo.sum() < fo.size
