@@ -446,6 +446,19 @@ def run_gpu(args, rank, world, local):
             "value": round(v, 3), "unit": "MLUPS", "cores": p, "kind": "port",
             "sample": f"{steps} lattice steps of the full workload "
                       f"({el:.1f} s), {p} z-slab ranks on {p} threads"}
+    if rank == 0 and world == 1 and not args.no_extras:
+        # the rest of the metric: served permeability solves (solves/s and
+        # latency, answers against FP64) and the batched pool against the
+        # plain kernel; bounded runs of the serving and batched workloads
+        t0 = time.perf_counter()
+        line["served"] = served_result(args.extra_requests, args.extra_rate,
+                                       args.budget_gb, args.serve_precision,
+                                       args.check_every, args.max_steps,
+                                       max_wall=args.extra_wall, fp64_check=0,
+                                       plain_fp64=True)
+        line["batched"] = batched_result(args.samples, args.check_every,
+                                         args.max_steps, args.plain_steps)
+        line["extras_wall_s"] = round(time.perf_counter() - t0, 1)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -524,15 +537,17 @@ def run_pool(args):
     print(json.dumps(line), flush=True)
 
 
-def run_batched(args):
+def batched_result(n_samples, K, max_steps, plain_steps):
+    """The batched workload (n_samples samples of seed 3, FP32 storage, each
+    to its 1e-7 steady-state test) in one pool, against looping the plain
+    FP32 kernel over the samples, with each sample's permeability against
+    the FP64 pool's."""
     import torch
     import porelb_gb300 as P
     from porelb_gb300.workloads import batched_samples
-    torch.cuda.set_device(0)
-    samples = batched_samples(args.samples, 3)
-    K = args.check_every
-    res32, ns32, wall32 = _steady_batch(samples, "fp32", K, args.max_steps)
-    res64, ns64, wall64 = _steady_batch(samples, "fp64", K, args.max_steps)
+    samples = batched_samples(n_samples, 3)
+    res32, ns32, wall32 = _steady_batch(samples, "fp32", K, max_steps)
+    res64, ns64, wall64 = _steady_batch(samples, "fp64", K, max_steps)
     # plain kernel per sample (FP32), timed on a fixed step count, then the
     # loop over samples is costed with each sample's own step count
     loop_s = 0.0
@@ -545,27 +560,35 @@ def run_batched(args):
         sim.step(20)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.step(args.plain_steps, it_begin=20)
+        sim.step(plain_steps, it_begin=20)
         el = time.perf_counter() - t0
         sim.close()
-        loop_s += el / args.plain_steps * res32[smp.index]["steps"]
+        loop_s += el / plain_steps * res32[smp.index]["steps"]
     errs = [abs(res32[i]["k_darcy"] - res64[i]["k_darcy"]) /
             abs(res64[i]["k_darcy"]) for i in res32 if res64[i]["k_darcy"]]
     conv = sum(1 for r in res32.values() if r["status"] == 1)
-    line = {
+    return {
         "metric": "fluid MLUPS (batched, FP32)",
         "value": round(ns32 / wall32 / 1e6, 1), "unit": "MLUPS",
         "plain_loop_mlups": round(ns32 / loop_s / 1e6, 1),
         "speedup_vs_plain_loop": round(loop_s / wall32, 3),
         "fp64_batched_mlups": round(ns64 / wall64 / 1e6, 1),
         "samples": len(samples), "converged": conv,
-        "k_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs)},
+        "k_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs),
+                              "within_1e-3": sum(e <= 1e-3 for e in errs),
+                              "of": len(errs)},
         "wall_s": round(wall32, 2), "check_every": K,
-        "config": {"workload": "batched 64 samples, seed 3",
+        "config": {"workload": f"batched {len(samples)} samples, seed 3",
                    "edges": [s.edge for s in samples],
-                   "tol": 1e-7, "force": 1e-6, "max_steps": args.max_steps},
+                   "tol": 1e-7, "force": 1e-6, "max_steps": max_steps},
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_batched(args):
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(batched_result(args.samples, args.check_every, args.max_steps,
+                                    args.plain_steps)), flush=True)
 
 
 def _plain_fp64_fcfs(reqs, K, max_steps):
@@ -611,53 +634,66 @@ SERVE_FORMS = {"fp16dev": "FP16 deviations", "bf16dev": "BF16 deviations",
                "fp32": "FP32", "fp64": "FP64"}
 
 
-def run_served(args):
-    import torch
+def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
+                  max_wall=None, fp64_check=32, plain_fp64=False):
+    """The serving workload (n_requests Poisson requests of seed 4 at `rate`
+    per second) through the continuous-batching server, with the
+    permeabilities checked against FP64: a pooled FP64 solve of the first
+    fp64_check answered requests, and with plain_fp64 the FP64 plain form
+    serving every answered request one at a time (first come first
+    served), which also gives that form's solves/s and latencies."""
     from porelb_gb300.serve import Server
     from porelb_gb300.workloads import serving_requests
-    torch.cuda.set_device(0)
-    reqs = serving_requests(args.requests, 4, args.rate)
-    srv = Server(args.budget_gb * 1e9, args.serve_precision,
-                 check_every=args.check_every)
-    done, summ = srv.serve(reqs, max_wall=args.max_wall)
+    reqs = serving_requests(n_requests, 4, rate)
+    srv = Server(budget_gb * 1e9, precision, check_every=K)
+    done, summ = srv.serve(reqs, max_wall=max_wall)
     srv.close()
-    # FP64 plain form on a sample of the same requests, one at a time
-    sub = [r for r in reqs if any(d["index"] == r.index for d in done)][: args.fp64_check]
-    res64, ns64, wall64 = _steady_batch(sub, "fp64", args.check_every,
-                                        args.max_steps)
     by = {d["index"]: d for d in done}
+    sub = [r for r in reqs if r.index in by][:fp64_check]
+    res64, ns64, wall64 = (_steady_batch(sub, "fp64", K, max_steps) if sub
+                           else ({}, 0, 0.0))
     errs = [abs(by[i]["k_darcy"] - r["k_darcy"]) / abs(r["k_darcy"])
             for i, r in res64.items() if r["k_darcy"]]
     plain = None
-    if args.plain_fp64:
+    if plain_fp64:
         served = [r for r in reqs if r.index in by]
-        ks64, plain = _plain_fp64_fcfs(served, args.check_every, args.max_steps)
+        ks64, plain = _plain_fp64_fcfs(served, K, max_steps)
         perr = [abs(by[i]["k_darcy"] - k) / abs(k) for i, k in ks64.items() if k]
         plain["k_rel_err_served_vs_plain_fp64"] = {
             "max": max(perr) if perr else None,
             "median": statistics.median(perr) if perr else None,
             "within_1e-3": sum(e <= 1e-3 for e in perr), "of": len(perr)}
-    line = {
-        "metric": "perm solves/s (served, %s)" % SERVE_FORMS[args.serve_precision],
+    return {
+        "metric": "perm solves/s (served, %s)" % SERVE_FORMS[precision],
         "value": round(summ["solves_per_s"], 3), "unit": "solves/s",
         "p50_latency_s": round(summ["p50_latency_s"], 3),
         "p99_latency_s": round(summ["p99_latency_s"], 3),
         "fluid_mlups": round(summ["fluid_mlups"], 1),
         "requests_done": summ["requests"], "requests": len(reqs),
+        "rejected": len(summ["rejected"]),
         "k_rel_err_vs_fp64": {"checked": len(errs),
                               "max": max(errs) if errs else None,
-                              "median": statistics.median(errs) if errs else None},
+                              "median": statistics.median(errs) if errs else None,
+                              "within_1e-3": sum(e <= 1e-3 for e in errs)},
         "fp64_mlups_on_checked": round(ns64 / wall64 / 1e6, 1) if wall64 else None,
         "plain_fp64_fcfs": plain,
         "time_split_s": {"admission": round(summ["admit_s"], 2),
                          "batch_run": round(summ["run_s"], 2),
                          "wall": round(summ["wall_s"], 2)},
         "config": {"workload": f"{len(reqs)} Poisson requests, seed 4",
-                   "rate_per_s": args.rate, "budget_gb": args.budget_gb,
-                   "check_every": args.check_every,
+                   "rate_per_s": rate, "budget_gb": budget_gb,
+                   "check_every": K, "storage": precision,
                    "capacity_nodes": summ["capacity_nodes"]},
     }
-    print(json.dumps(line), flush=True)
+
+
+def run_served(args):
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(served_result(args.requests, args.rate, args.budget_gb,
+                                   args.serve_precision, args.check_every,
+                                   args.max_steps, args.max_wall, args.fp64_check,
+                                   args.plain_fp64)), flush=True)
 
 
 def run_precision(args):
@@ -746,6 +782,13 @@ def main():
                     help="also serve the same requests with the FP64 plain "
                          "form, one at a time (first come first served)")
     ap.add_argument("--edge", type=int, default=1024)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the served and batched runs of the default line")
+    ap.add_argument("--extra-requests", type=int, default=200,
+                    help="requests of the served run in the default line")
+    ap.add_argument("--extra-rate", type=float, default=20.0)
+    ap.add_argument("--extra-wall", type=float, default=120.0,
+                    help="wall-clock cap of the served run in the default line")
     args = ap.parse_args()
     if args.mode == "batched":
         return run_batched(args)
