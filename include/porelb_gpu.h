@@ -218,6 +218,10 @@ int plb_save_parts(plb_sim *sim, const char *dir, int tag);
 int plb_get_f(plb_sim *sim, double *f_aos);
 /* Overwrite the state from a reference-order AoS array. */
 int plb_set_f(plb_sim *sim, const double *f_aos);
+/* The distributions the next step will collide, after its stream: the
+ * reference's f1 after the next stream_inner_nodes (porelb.c:285-300) of
+ * the current f0, AoS, reference node order, FP64. */
+int plb_get_f_streamed(plb_sim *sim, double *f_aos);
 
 /* FP64 sums over the last step's macros: sum of Ux and of Rho. */
 int plb_reduce(plb_sim *sim, double *sum_ux, double *mass);

@@ -109,6 +109,7 @@ _SIGS = {
                             ctypes.POINTER(ctypes.c_longlong),
                             ctypes.POINTER(ctypes.c_size_t)]),
     "plb_kernel_flags": (_I, [_P, ctypes.POINTER(ctypes.c_uint)]),
+    "plb_get_f_streamed": (_I, [_P, _P]),
     "plb_batch_sample_nodes": (_I, [_P, _I, _IP]),
     "plb_batch_free_nodes": (_I, [_P, ctypes.POINTER(ctypes.c_longlong),
                                   ctypes.POINTER(ctypes.c_longlong)]),

@@ -214,6 +214,13 @@ class Simulation:
         _check(self._lib.plb_get_f(self._h, _ptr(out)), "get_f")
         return out
 
+    def get_f_streamed(self):
+        """The distributions the next step collides, after its stream (the
+        reference's f1 after the next stream), AoS in reference order."""
+        out = np.empty(self.N * Q, dtype=np.float64)
+        _check(self._lib.plb_get_f_streamed(self._h, _ptr(out)), "get_f_streamed")
+        return out
+
     def set_f(self, f_aos):
         a = np.ascontiguousarray(f_aos, dtype=np.float64).reshape(-1)
         if a.size != self.N * Q:

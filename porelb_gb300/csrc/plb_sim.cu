@@ -418,6 +418,26 @@ __global__ void k_get_f_dev(const T *f, const int *perm, long long npad, int n,
     }
 }
 
+/* the next step's streamed values (through the pull words), FP64 AoS */
+template <typename T>
+__global__ void k_get_streamed(const T *f, const uint32_t *nbr, const int *perm,
+                               long long npad, int n, float inv_scale, double *out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long o = (long long)perm[k] * Q;
+#pragma unroll
+    for (int j = 0; j < Q; j++) {
+        const long long at = j == 0 ? k : (long long)j * npad + (int)nbr[(j - 1) * npad + k];
+        if constexpr (sizeof(T) == 8) {
+            out[o + j] = ((const double *)f)[at];
+        } else {
+            const double g = load_dev(f + at) * (double)inv_scale;
+            out[o + j] = wq(j) + wq(j) * g;
+        }
+    }
+}
+
 __global__ void k_set_f_fp64(double *f, const int *perm, long long npad, int n,
                              const double *in)
 {
@@ -1063,6 +1083,37 @@ int plb_set_f(plb_sim *s, const double *f_aos)
     cudaFree(d);
     if (e != cudaSuccess) {
         fprintf(stderr, "porelb_gpu: set_f failed: %s\n", cudaGetErrorString(e));
+        return PLB_ERR_CUDA;
+    }
+    return PLB_OK;
+}
+
+int plb_get_f_streamed(plb_sim *s, double *f_aos)
+{
+    if (!s || (!f_aos && s->n > 0)) return PLB_ERR_ARG;
+    if (!s->initialized) return PLB_ERR_STATE;
+    if (s->n == 0) return PLB_OK;
+    CK(cudaSetDevice(s->device));
+    double *d = nullptr;
+    const size_t bytes = sizeof(double) * Q * (size_t)s->n;
+    CK(cudaMalloc(&d, bytes));
+    const unsigned g = nblk(s->n, 256);
+    const void *f = s->f[s->cur];
+    const float inv = 1.0f / s->scale;
+    switch (s->precision) {
+    case PLB_FP64_EXACT:
+    case PLB_FP64:
+    case PLB_FP64_FMA: k_get_streamed<double><<<g, 256, 0, s->stream>>>((const double *)f, s->nbr, s->perm, s->npad, s->n, inv, d); break;
+    case PLB_FP32: k_get_streamed<float><<<g, 256, 0, s->stream>>>((const float *)f, s->nbr, s->perm, s->npad, s->n, inv, d); break;
+    case PLB_FP16DEV: k_get_streamed<__half><<<g, 256, 0, s->stream>>>((const __half *)f, s->nbr, s->perm, s->npad, s->n, inv, d); break;
+    default: k_get_streamed<__nv_bfloat16><<<g, 256, 0, s->stream>>>((const __nv_bfloat16 *)f, s->nbr, s->perm, s->npad, s->n, inv, d); break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f_aos, d, bytes, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "porelb_gpu: get_f_streamed failed: %s\n", cudaGetErrorString(e));
         return PLB_ERR_CUDA;
     }
     return PLB_OK;

@@ -371,3 +371,33 @@ def test_dropin_porelb_x_dumps_match_reference(tmp_path):
     for fn, h in m["parts"].items():
         with open(tmp_path / fn, "rb") as fh:
             assert hashlib.sha256(fh.read()).hexdigest() == h, fn
+
+
+@pytest.mark.parametrize("num_p,halfway", [(1, False), (3, False), (1, True)])
+def test_streamed_state_equals_reference_next_stream(num_p, halfway):
+    """plb_get_f_streamed is what the reference's f1 holds after one more
+    stream of the current f0 (stream_inner_nodes, porelb.c:285-300, with its
+    double-written and never-written slots; with num_p > 1 the halo order
+    of porelb.c:428-433), computed from the oracle's pull table."""
+    dims = (12, 9, 9)
+    flag = noise_flag(dims, 0.3, 17)
+    V, vs = P.build_table(flag, *dims, num_p)
+    f0, _, _ = O.pull_run(V, vs, 0.8, 1e-3, 7, remote_wins=num_p > 1, halfway=halfway)
+    kind, src = O.pull_table(V, vs, num_p > 1, halfway)
+    N = len(V)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    g = f0.reshape(N, 19)
+    f1 = np.tile(w, (N, 1))
+    f1[:, 0] = g[:, 0]
+    opp = [0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17]
+    k, sidx = kind.reshape(N, 18), src.reshape(N, 18)
+    for j in range(1, 19):
+        pull, bnc = k[:, j - 1] == 0, k[:, j - 1] == 1
+        f1[pull, j] = g[sidx[pull, j - 1], j]
+        f1[bnc, j] = g[bnc, opp[j]]
+    with P.Simulation(V, *dims, vs, tau=0.8, force=1e-3, precision="fp64_exact",
+                      boundary="halfway" if halfway else "reference") as sim:
+        sim.init_dist_macro()
+        sim.step(7)
+        assert (sim.get_f() == f0).all()
+        assert (sim.get_f_streamed() == f1.reshape(-1)).all()
