@@ -677,9 +677,13 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
                               "within_1e-3": sum(e <= 1e-3 for e in errs)},
         "fp64_mlups_on_checked": round(ns64 / wall64 / 1e6, 1) if wall64 else None,
         "plain_fp64_fcfs": plain,
-        "time_split_s": {"admission": round(summ["admit_s"], 2),
-                         "batch_run": round(summ["run_s"], 2),
+        "time_split_s": {"admission_overlapped": round(summ["admit_s"], 2),
+                         "waiting_for_intervals": round(summ["wait_s"], 2),
+                         "gpu_busy": round(summ["gpu_busy_s"], 2),
                          "wall": round(summ["wall_s"], 2)},
+        "gpu_idle_frac": (round(summ["gpu_idle_frac"], 4)
+                          if summ["gpu_idle_frac"] is not None else None),
+        "handoffs": summ["handoffs"], "handoff_tol": summ["handoff_tol"],
         "config": {"workload": f"{len(reqs)} Poisson requests, seed 4",
                    "rate_per_s": rate, "budget_gb": budget_gb,
                    "check_every": K, "storage": precision,

@@ -262,7 +262,10 @@ typedef struct {
     double force_x;      /* body force of the sample */
     double tol;          /* steady-state tolerance on <u_x> over one interval */
     long long max_steps; /* stop after this many steps (<= 0: no limit) */
-    int reserved[4];
+    double handoff_tol;  /* > tol: park the sample (status 4, blocks kept)
+                            once its change is below this, for
+                            plb_batch_transfer; 0 = never */
+    int reserved[2];
 } plb_sample_params;
 
 /* Device bytes per pool node for a storage form (the admission unit). */
@@ -281,11 +284,31 @@ int plb_batch_add_packed(plb_batch *b, uint64_t seed, int nx, int ny, int nz,
                          double rmin, double rmax, double porosity,
                          const plb_sample_params *sp, int *id,
                          int *num_spheres, double *porosity_out);
-/* Run `intervals` intervals of K steps (stops early when nothing is active). */
+/* Run `intervals` intervals of K steps (stops early when nothing is active):
+ * plb_batch_launch + plb_batch_finish each. */
 int plb_batch_run(plb_batch *b, int intervals, int *n_active);
+/* Start one interval on the pool's stream and return (*n_active: samples it
+ * steps; 0 = nothing launched).  While it runs the caller may admit samples
+ * (built on a second stream; they join at the next launch), poll, read
+ * results and transfer parked samples; plb_batch_get_f / get_macros and
+ * releasing a sample the interval steps return PLB_ERR_STATE. */
+int plb_batch_launch(plb_batch *b, int *n_active);
+/* Wait for the interval in flight, then check every sample it stepped:
+ * converged, step limit, density guard or handoff tolerance. */
+int plb_batch_finish(plb_batch *b);
+/* Admit into dst a sample parked in src (same device and K; deviation
+ * storage forms): its node table and current state, converted to dst's
+ * storage form, with its step count and convergence history, which the
+ * steady-state test continues from.  The caller then releases it in src.
+ * No reference counterpart. */
+int plb_batch_transfer(plb_batch *src, int id, plb_batch *dst, int *new_id);
+/* Device time of the last completed interval (CUDA events around its graph
+ * on the pool's stream), in milliseconds. */
+int plb_batch_interval_ms(plb_batch *b, float *ms);
 /* Ids of samples that finished since the last poll. */
 int plb_batch_poll(plb_batch *b, int *ids, int max_ids, int *count);
-/* status: 0 running, 1 converged, 2 step limit, 3 released, <0 error. */
+/* status: 0 running, 1 converged, 2 step limit, 3 released, 4 parked at the
+ * handoff tolerance, <0 error. */
 int plb_batch_result(plb_batch *b, int id, double *k_darcy, double *mean_ux,
                      long long *steps, int *status);
 int plb_batch_release(plb_batch *b, int id);

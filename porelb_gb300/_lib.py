@@ -46,7 +46,7 @@ class Params(ctypes.Structure):
 class SampleParams(ctypes.Structure):
     _fields_ = [("tau", ctypes.c_double), ("force_x", ctypes.c_double),
                 ("tol", ctypes.c_double), ("max_steps", ctypes.c_longlong),
-                ("reserved", ctypes.c_int * 4)]
+                ("handoff_tol", ctypes.c_double), ("reserved", ctypes.c_int * 2)]
 
 
 _P = ctypes.c_void_p
@@ -98,6 +98,10 @@ _SIGS = {
                                   ctypes.POINTER(SampleParams), _IP, _IP,
                                   _DP]),
     "plb_batch_run": (_I, [_P, _I, _IP]),
+    "plb_batch_launch": (_I, [_P, _IP]),
+    "plb_batch_finish": (_I, [_P]),
+    "plb_batch_transfer": (_I, [_P, _I, _P, _IP]),
+    "plb_batch_interval_ms": (_I, [_P, ctypes.POINTER(ctypes.c_float)]),
     "plb_batch_poll": (_I, [_P, _IP, _I, _IP]),
     "plb_batch_result": (_I, [_P, _I, _DP, _DP,
                               ctypes.POINTER(ctypes.c_longlong), _IP]),

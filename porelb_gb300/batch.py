@@ -13,7 +13,9 @@ import numpy as np
 from . import _lib
 from .api import PRECISIONS, PorelbError, _check, _ptr
 
-STATUS = {0: "running", 1: "converged", 2: "step limit", 3: "released"}
+STATUS = {0: "running", 1: "converged", 2: "step limit", 3: "released",
+          4: "parked"}
+PARKED = 4
 
 
 class Batch:
@@ -36,15 +38,17 @@ class Batch:
                                                     int(keep_macros))
 
     @staticmethod
-    def _sp(tau, force, tol, max_steps):
+    def _sp(tau, force, tol, max_steps, handoff_tol=0.0):
         sp = _lib.SampleParams()
         sp.tau, sp.force_x, sp.tol, sp.max_steps = tau, force, tol, max_steps
+        sp.handoff_tol = handoff_tol
         return sp
 
-    def add_flag(self, flag, nx, ny, nz, tau, force, tol=1e-7, max_steps=0):
+    def add_flag(self, flag, nx, ny, nz, tau, force, tol=1e-7, max_steps=0,
+                 handoff_tol=0.0):
         flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
         sid = ctypes.c_int(-1)
-        sp = self._sp(tau, force, tol, max_steps)
+        sp = self._sp(tau, force, tol, max_steps, handoff_tol)
         _check(self._lib.plb_batch_add_flag(self._h, _ptr(flag), nx, ny, nz,
                                             ctypes.byref(sp),
                                             ctypes.byref(sid)),
@@ -53,11 +57,11 @@ class Batch:
         return sid.value
 
     def add_packed(self, seed, nx, ny, nz, rmin, rmax, porosity, tau, force,
-                   tol=1e-7, max_steps=0):
+                   tol=1e-7, max_steps=0, handoff_tol=0.0):
         sid = ctypes.c_int(-1)
         ns = ctypes.c_int(0)
         phi = ctypes.c_double(0.0)
-        sp = self._sp(tau, force, tol, max_steps)
+        sp = self._sp(tau, force, tol, max_steps, handoff_tol)
         _check(self._lib.plb_batch_add_packed(
             self._h, ctypes.c_uint64(seed), nx, ny, nz, rmin, rmax, porosity,
             ctypes.byref(sp), ctypes.byref(sid), ctypes.byref(ns),
@@ -70,6 +74,40 @@ class Batch:
         """add_packed, or None when the pool has no room (PLB_ERR_NOMEM)."""
         try:
             return self.add_packed(*args, **kw)
+        except PorelbError as e:
+            if e.status == _lib.ERR_NOMEM:
+                return None
+            raise
+
+    def launch(self):
+        """Start one interval without waiting; returns the samples it steps
+        (0: nothing launched)."""
+        act = ctypes.c_int(0)
+        _check(self._lib.plb_batch_launch(self._h, ctypes.byref(act)), "plb_batch_launch")
+        return act.value
+
+    def finish(self):
+        """Wait for the interval in flight and check its samples."""
+        _check(self._lib.plb_batch_finish(self._h), "plb_batch_finish")
+
+    def interval_ms(self):
+        """Device time of the last completed interval (ms)."""
+        ms = ctypes.c_float(0.0)
+        _check(self._lib.plb_batch_interval_ms(self._h, ctypes.byref(ms)), "interval_ms")
+        return ms.value
+
+    def transfer(self, sid, dst):
+        """Move parked sample sid into pool dst (converting its storage);
+        returns its id there.  The caller releases it here."""
+        nid = ctypes.c_int(-1)
+        _check(self._lib.plb_batch_transfer(self._h, sid, dst._h, ctypes.byref(nid)),
+               "plb_batch_transfer")
+        return nid.value
+
+    def try_transfer(self, sid, dst):
+        """transfer, or None when dst has no room (PLB_ERR_NOMEM)."""
+        try:
+            return self.transfer(sid, dst)
         except PorelbError as e:
             if e.status == _lib.ERR_NOMEM:
                 return None

@@ -6,13 +6,18 @@
  * scale the step applies (k_batch_step, plb_step.cu).  All samples advance
  * together: one launch per lattice step covers every active block, and an
  * interval of K steps (the last writing the per-block sums) plus the
- * per-sample reduction is captured once in a CUDA graph and replayed.
- * After each interval the host checks each sample's steady-state criterion
- * (relative change of the mean u_x over the interval), retires converged
- * samples and frees their blocks; new samples are admitted at interval
- * boundaries into free block ranges (first fit).  A sample's arithmetic does
- * not depend on what else is in the pool, so its result is the same alone
- * and in a mix.
+ * per-sample reduction is one CUDA graph, built once and replayed;
+ * admissions and retirements only change the active-block list and the
+ * grid of the step nodes.  An interval is launched asynchronously
+ * (plb_batch_launch) and completed by plb_batch_finish, which checks each
+ * sample's steady-state criterion (relative change of the mean u_x over
+ * the interval), retires converged samples and frees their blocks.
+ * Samples admitted while an interval runs are built on a second stream into
+ * free block ranges (first fit) and join at the next launch.  A sample may
+ * instead be parked at a looser handoff tolerance, keeping its blocks, and
+ * moved into another pool (plb_batch_transfer), e.g. from 16-bit to FP32
+ * storage.  A sample's arithmetic does not depend on what else is in the
+ * pool, so its result is the same alone and in a mix.
  *
  * The reference has no batching; each sample follows its own step loop
  * (porelb.c:426-437) with the it > 0 half-force rule counted from the
@@ -179,11 +184,51 @@ __global__ void k_get_macro_sample(const double *macro, long long npad, long lon
     for (int c = 0; c < 4; c++) out[c * (long long)n + o] = macro[c * npad + i];
 }
 
+/* a sample's node table moved into another pool: pull words re-based */
+__global__ void k_translate_words(const uint32_t *src, long long snp, long long sbase,
+                                  uint32_t srest, uint32_t *dst, long long dnp,
+                                  long long dbase, uint32_t drest, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    for (int j = 1; j < Q; j++) {
+        const uint32_t w = src[(long long)(j - 1) * snp + sbase + k];
+        uint32_t o;
+        if (w == srest) o = drest;
+        else if ((long long)(uint32_t)(w - (uint32_t)sbase) < (long long)n)
+            o = (uint32_t)(dbase + (long long)(w - (uint32_t)sbase));
+        else o = bounce_word(j, dbase + k, dnp);
+        dst[(long long)(j - 1) * dnp + dbase + k] = o;
+    }
+}
+
+/* a sample's stored deviations moved into another storage form: g =
+ * stored / scale_in, stored again as g * scale_out */
+template <typename TI, typename TO>
+__global__ void k_convert_dev(const TI *in, long long inp, long long ibase, float inv_in,
+                              TO *out, long long onp, long long obase, float scale_out,
+                              int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    for (int j = 0; j < Q; j++) {
+        const float g = (float)ld_dev<TI>(in + j * inp + ibase + k) * inv_in;
+        const float h = g * scale_out;
+        TO *p = out + j * onp + obase + k;
+        if constexpr (std::is_same<TO, float>::value) *p = h;
+        else if constexpr (std::is_same<TO, __half>::value) *p = __float2half_rn(h);
+        else *p = __float2bfloat16_rn(h);
+    }
+}
+
 struct SampleHost {
     int used = 0, active = 0, finished = 0;
+    int parked = 0;    /* stopped at the handoff tolerance, blocks kept */
+    int stepping = 0;  /* stepped by the interval in flight */
+    int pending = 0;   /* admitted; joins at the next launch */
     long long blk0 = 0, nblk = 0;
     int n = 0, nx = 0, ny = 0, nz = 0;
-    double tau = 0, force = 0, tol = 0, nu = 0;
+    double tau = 0, force = 0, tol = 0, nu = 0, handoff_tol = 0;
     long long max_steps = 0;
     long long start = 0, steps = 0;
     int checks = 0;
@@ -201,6 +246,10 @@ struct plb_batch {
     int device = 0, precision = 0, K = 1000, keep_macros = 0, max_samples = 0;
     size_t elem = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t adm = nullptr; /* admissions, concurrent with an interval */
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr; /* around the interval in flight */
+    float last_ms = 0.f;
+    bool in_flight = false;
     long long cap_blocks = 0, npad = 0, rest = 0;
     void *f[2] = {nullptr, nullptr};
     int cur = 0;
@@ -226,8 +275,10 @@ struct plb_batch {
     std::vector<int> done;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    long long graph_n = -1;
     int graph_cur = -1;
+    int graph_grid = 0;                     /* grid of the step nodes */
+    std::vector<BatchArgs> step_args;       /* kernel arguments per step node */
+    std::vector<cudaGraphNode_t> step_nodes;
     size_t bytes = 0;
 };
 
@@ -271,6 +322,9 @@ static void batch_free(plb_batch *b)
     if (b->h_ssum) cudaFreeHost(b->h_ssum);
     if (b->h_serr) cudaFreeHost(b->h_serr);
     if (b->st) cudaStreamDestroy(b->st);
+    if (b->adm) cudaStreamDestroy(b->adm);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
     delete b;
 }
 
@@ -279,6 +333,7 @@ void plb_batch_destroy(plb_batch *b)
     if (!b) return;
     cudaSetDevice(b->device);
     if (b->st) cudaStreamSynchronize(b->st);
+    if (b->adm) cudaStreamSynchronize(b->adm);
     batch_free(b);
 }
 
@@ -309,6 +364,9 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
     b->s.resize((size_t)max_samples);
     b->free_blocks[0] = b->cap_blocks;
     cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->adm, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     auto al = [&](auto **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc((void **)p, bytes ? bytes : 16);
         b->bytes += bytes;
@@ -380,6 +438,17 @@ static void free_range(plb_batch *b, long long start, long long len)
     }
 }
 
+/* A sample whose tables and state are in place joins the pool: at once
+ * when no interval runs, else at the next launch (the interval in flight
+ * must not see it). */
+static void activate(plb_batch *b, int sid)
+{
+    SampleHost &h = b->s[sid];
+    h.active = 1;
+    h.pending = 1;
+    b->list_dirty = true;
+}
+
 /* Admit a sample whose flag grid is on the device. */
 static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
                      const plb_sample_params *sp, int *id)
@@ -396,7 +465,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     if (cudaMalloc(&lexbits, words * 4) != cudaSuccess ||
         cudaMalloc(&lexoffs, words * 4) != cudaSuccess)
         rc = PLB_ERR_NOMEM;
-    if (rc == PLB_OK) rc = flag_rank(dflag, nx, ny, nz, 1, lexbits, lexoffs, &n, &slab0, b->st);
+    if (rc == PLB_OK) rc = flag_rank(dflag, nx, ny, nz, 1, lexbits, lexoffs, &n, &slab0, b->adm);
     if (rc == PLB_OK) {
         nblk = (n + B - 1) / B;
         if (nblk == 0) nblk = 1;
@@ -407,7 +476,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
         const long long base = blk0 * B;
         rc = flag_tables(dflag, nx, ny, nz, 1, PLB_ORDER_MORTON, 0, 0, lexbits, lexoffs, n,
                          b->npad, b->perm + base, b->coord + base, b->nbr + base,
-                         (uint32_t)base, (uint32_t)b->rest, b->st);
+                         (uint32_t)base, (uint32_t)b->rest, b->adm);
         if (rc != PLB_OK) free_range(b, blk0, nblk);
     }
     cudaFree(lexbits);
@@ -417,7 +486,6 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     SampleHost &h = b->s[sid];
     h = SampleHost();
     h.used = 1;
-    h.active = 1;
     h.blk0 = blk0;
     h.nblk = nblk;
     h.n = n;
@@ -425,6 +493,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     h.tau = sp->tau;
     h.force = sp->force_x;
     h.tol = sp->tol;
+    h.handoff_tol = sp->handoff_tol > sp->tol ? sp->handoff_tol : 0.0;
     h.max_steps = sp->max_steps > 0 ? sp->max_steps : (1LL << 40);
     h.nu = 1.0 / 3.0 * (sp->tau - 0.5);
     h.start = b->t;
@@ -442,18 +511,18 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     make_coeffs(sp->tau, sp->force_x, h.scale, &d.co);
     d.base = blk0 * B;
     d.n = n;
-    d.start = (int)b->t;
-    const int one = 1;
-    BCK(cudaMemcpyAsync(b->sdev + sid, &d, sizeof(d), cudaMemcpyHostToDevice, b->st));
-    BCK(cudaMemcpyAsync(b->sactive + sid, &one, 4, cudaMemcpyHostToDevice, b->st));
-    BCK(cudaMemsetAsync(b->serr + sid, 0, 4, b->st));
+    /* a sample admitted while an interval runs starts after it */
+    d.start = (int)(b->t + (b->in_flight ? b->K : 0));
+    h.start = d.start;
+    BCK(cudaMemcpyAsync(b->sdev + sid, &d, sizeof(d), cudaMemcpyHostToDevice, b->adm));
+    BCK(cudaMemsetAsync(b->serr + sid, 0, 4, b->adm));
     if (n > 0)
-        k_fill_rest<<<gb(n, B), B, 0, b->st>>>(b->f[0], b->f[1], b->npad, d.base, d.base + n,
-                                              (int)b->elem);
-    k_set_blocks<<<gb(nblk, B), B, 0, b->st>>>(b->blk, blk0, nblk, sid, n);
+        k_fill_rest<<<gb(n, B), B, 0, b->adm>>>(b->f[0], b->f[1], b->npad, d.base, d.base + n,
+                                               (int)b->elem);
+    k_set_blocks<<<gb(nblk, B), B, 0, b->adm>>>(b->blk, blk0, nblk, sid, n);
     BCK(cudaGetLastError());
-    BCK(cudaStreamSynchronize(b->st));
-    b->list_dirty = true;
+    BCK(cudaStreamSynchronize(b->adm));
+    activate(b, sid);
     *id = sid;
     return PLB_OK;
 }
@@ -469,10 +538,10 @@ int plb_batch_add_flag(plb_batch *b, const uint8_t *flag, int nx, int ny, int nz
     uint8_t *d = nullptr;
     BCK(cudaMalloc(&d, cells));
     int rc = PLB_OK;
-    if (cudaMemcpyAsync(d, flag, cells, cudaMemcpyHostToDevice, b->st) != cudaSuccess)
+    if (cudaMemcpyAsync(d, flag, cells, cudaMemcpyHostToDevice, b->adm) != cudaSuccess)
         rc = PLB_ERR_CUDA;
     if (rc == PLB_OK) rc = add_dflag(b, d, nx, ny, nz, sp, id);
-    cudaStreamSynchronize(b->st);
+    cudaStreamSynchronize(b->adm);
     cudaFree(d);
     return rc;
 }
@@ -491,15 +560,18 @@ int plb_batch_add_packed(plb_batch *b, uint64_t seed, int nx, int ny, int nz,
     uint8_t *d = nullptr;
     BCK(cudaMalloc(&d, cells));
     int rc = sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, d, num_spheres,
-                                porosity_out, b->st);
+                                porosity_out, b->adm);
     if (rc == PLB_OK) rc = add_dflag(b, d, nx, ny, nz, sp, id);
-    cudaStreamSynchronize(b->st);
+    cudaStreamSynchronize(b->adm);
     cudaFree(d);
     return rc;
 }
 
-/* Capture one interval: K steps (the last writes the sums), the step
- * counter advance, the per-sample reduction and its read-back. */
+/* Build the interval graph: K batch-step kernel nodes in a chain (the last
+ * writes the sums), the step counter advance, the per-sample reduction and
+ * its read-back.  The step nodes' grid is the active-block count; when the
+ * active list changes only their grid is updated (set_graph_grid), so
+ * admissions and retirements never rebuild the graph. */
 static int build_graph(plb_batch *b)
 {
     if (b->gexec) {
@@ -510,8 +582,6 @@ static int build_graph(plb_batch *b)
         cudaGraphDestroy(b->graph);
         b->graph = nullptr;
     }
-    const int nb = (int)b->hlist.size();
-    BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     BatchArgs a;
     memset(&a, 0, sizeof(a));
     a.nbr = b->nbr;
@@ -527,131 +597,366 @@ static int build_graph(plb_batch *b)
     a.macro = b->macro;
     a.partial = b->partial;
     a.serr = b->serr;
+    int bt = 0;
+    const void *fn = batch_step_kernel(b->precision, false, &bt);
+    const void *fn_m = batch_step_kernel(b->precision, true, &bt);
+    b->step_args.assign((size_t)b->K, a);
+    b->step_nodes.assign((size_t)b->K, nullptr);
+    b->graph_grid = (int)b->hlist.size() * h;
+    cudaError_t e = cudaGraphCreate(&b->graph, 0);
+    cudaGraphNode_t prev = nullptr;
     int cur = b->cur;
-    cudaError_t e = cudaSuccess;
     for (int k = 0; k < b->K && e == cudaSuccess; k++) {
-        a.fin = b->f[cur];
-        a.fout = b->f[cur ^ 1];
-        a.t_off = k;
-        e = launch_batch_step(b->precision, k == b->K - 1, a, nb, b->st);
+        BatchArgs &ak = b->step_args[(size_t)k];
+        ak.fin = b->f[cur];
+        ak.fout = b->f[cur ^ 1];
+        ak.t_off = k;
         cur ^= 1;
+        void *kp[1] = {&ak};
+        cudaKernelNodeParams p;
+        memset(&p, 0, sizeof(p));
+        p.func = (void *)(k == b->K - 1 ? fn_m : fn);
+        p.gridDim = dim3((unsigned)(b->graph_grid > 0 ? b->graph_grid : 1));
+        p.blockDim = dim3((unsigned)bt);
+        p.kernelParams = kp;
+        e = cudaGraphAddKernelNode(&b->step_nodes[(size_t)k], b->graph, prev ? &prev : nullptr,
+                                   prev ? 1 : 0, &p);
+        prev = b->step_nodes[(size_t)k];
+    }
+    int *t_dev = b->t_dev;
+    int K = b->K;
+    if (e == cudaSuccess) {
+        void *kp[2] = {&t_dev, &K};
+        cudaKernelNodeParams p;
+        memset(&p, 0, sizeof(p));
+        p.func = (void *)k_advance;
+        p.gridDim = dim3(1);
+        p.blockDim = dim3(1);
+        p.kernelParams = kp;
+        cudaGraphNode_t n = nullptr;
+        e = cudaGraphAddKernelNode(&n, b->graph, &prev, 1, &p);
+        prev = n;
+    }
+    const SampleDev *sd = b->sdev;
+    const int *sa = b->sactive;
+    const double *part = b->partial;
+    int nrows = (int)(h * b->cap_blocks);
+    int hh = h;
+    double *ssum = b->ssum;
+    if (e == cudaSuccess) {
+        void *kp[6] = {(void *)&sd, (void *)&sa, (void *)&part, &nrows, &hh, &ssum};
+        cudaKernelNodeParams p;
+        memset(&p, 0, sizeof(p));
+        p.func = (void *)k_sample_sums;
+        p.gridDim = dim3((unsigned)b->max_samples);
+        p.blockDim = dim3(128);
+        p.kernelParams = kp;
+        cudaGraphNode_t n = nullptr;
+        e = cudaGraphAddKernelNode(&n, b->graph, &prev, 1, &p);
+        prev = n;
     }
     if (e == cudaSuccess) {
-        k_advance<<<1, 1, 0, b->st>>>(b->t_dev, b->K);
-        k_sample_sums<<<b->max_samples, 128, 0, b->st>>>(b->sdev, b->sactive, b->partial,
-                                                         (int)(h * b->cap_blocks), h, b->ssum);
-        e = cudaGetLastError();
+        cudaGraphNode_t n = nullptr;
+        e = cudaGraphAddMemcpyNode1D(&n, b->graph, &prev, 1, b->h_ssum, b->ssum,
+                                     8 * 3 * (size_t)b->max_samples, cudaMemcpyDeviceToHost);
+        prev = n;
     }
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->h_ssum, b->ssum, 8 * 3 * (size_t)b->max_samples,
-                            cudaMemcpyDeviceToHost, b->st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->h_serr, b->serr, 4 * (size_t)b->max_samples,
-                            cudaMemcpyDeviceToHost, b->st);
-    cudaError_t e2 = cudaStreamEndCapture(b->st, &b->graph);
-    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) {
+        cudaGraphNode_t n = nullptr;
+        e = cudaGraphAddMemcpyNode1D(&n, b->graph, &prev, 1, b->h_serr, b->serr,
+                                     4 * (size_t)b->max_samples, cudaMemcpyDeviceToHost);
+    }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, b->graph, 0);
     if (e != cudaSuccess) {
-        fprintf(stderr, "porelb_gpu: batch graph capture failed: %s\n", cudaGetErrorString(e));
+        fprintf(stderr, "porelb_gpu: batch graph build failed: %s\n", cudaGetErrorString(e));
         return PLB_ERR_CUDA;
     }
-    b->graph_n = nb;
     b->graph_cur = b->cur;
     return PLB_OK;
 }
 
-static void retire(plb_batch *b, int sid, int status)
+/* The step nodes of the instantiated graph get the current active-block
+ * count as their grid. */
+static int set_graph_grid(plb_batch *b)
+{
+    const int h = batch_ctas_per_block(b->precision);
+    const int grid = (int)b->hlist.size() * h;
+    if (grid == b->graph_grid || grid == 0) return PLB_OK;
+    int bt = 0;
+    const void *fn = batch_step_kernel(b->precision, false, &bt);
+    const void *fn_m = batch_step_kernel(b->precision, true, &bt);
+    for (int k = 0; k < b->K; k++) {
+        void *kp[1] = {&b->step_args[(size_t)k]};
+        cudaKernelNodeParams p;
+        memset(&p, 0, sizeof(p));
+        p.func = (void *)(k == b->K - 1 ? fn_m : fn);
+        p.gridDim = dim3((unsigned)grid);
+        p.blockDim = dim3((unsigned)bt);
+        p.kernelParams = kp;
+        BCK(cudaGraphExecKernelNodeSetParams(b->gexec, b->step_nodes[(size_t)k], &p));
+    }
+    b->graph_grid = grid;
+    return PLB_OK;
+}
+
+/* The sample stops being stepped: it leaves the active list and its
+ * blocks are freed (or, parked at the handoff tolerance, kept until it is
+ * released). */
+static void retire(plb_batch *b, int sid, int status, bool keep_blocks = false)
 {
     SampleHost &h = b->s[sid];
     h.active = 0;
     h.finished = 1;
     h.status = status;
+    h.parked = keep_blocks ? 1 : 0;
     const int zero = 0;
     cudaMemcpyAsync(b->sactive + sid, &zero, 4, cudaMemcpyHostToDevice, b->st);
-    k_set_blocks<<<gb(h.nblk, B), B, 0, b->st>>>(b->blk, h.blk0, h.nblk, -1, 0);
-    free_range(b, h.blk0, h.nblk);
+    if (!keep_blocks) {
+        k_set_blocks<<<gb(h.nblk, B), B, 0, b->st>>>(b->blk, h.blk0, h.nblk, -1, 0);
+        free_range(b, h.blk0, h.nblk);
+    }
     b->list_dirty = true;
     b->done.push_back(sid);
+}
+
+int plb_batch_launch(plb_batch *b, int *n_active)
+{
+    if (!b) return PLB_ERR_ARG;
+    if (b->in_flight) return PLB_ERR_STATE;
+    BCK(cudaSetDevice(b->device));
+    int act = 0;
+    for (auto &h : b->s) act += h.active;
+    if (n_active) *n_active = act;
+    if (act == 0) return PLB_OK;
+    /* samples admitted since the last launch join now */
+    const int one = 1;
+    for (int sid = 0; sid < b->max_samples; sid++) {
+        SampleHost &h = b->s[sid];
+        if (h.pending) {
+            BCK(cudaMemcpyAsync(b->sactive + sid, &one, 4, cudaMemcpyHostToDevice, b->st));
+            h.pending = 0;
+        }
+        h.stepping = h.active;
+    }
+    if (b->list_dirty) {
+        /* the pool blocks of the active samples, in pool order */
+        std::vector<std::pair<long long, int>> order;
+        for (int sid = 0; sid < b->max_samples; sid++)
+            if (b->s[sid].active) order.emplace_back(b->s[sid].blk0, sid);
+        std::sort(order.begin(), order.end());
+        b->hlist.clear();
+        for (auto &o : order) {
+            const SampleHost &h = b->s[o.second];
+            for (long long k = 0; k < h.nblk; k++) b->hlist.push_back((int)(h.blk0 + k));
+        }
+        if (!b->hlist.empty())
+            BCK(cudaMemcpyAsync(b->blist, b->hlist.data(), 4 * b->hlist.size(),
+                                cudaMemcpyHostToDevice, b->st));
+        b->list_dirty = false;
+    }
+    if (!b->gexec || b->graph_cur != b->cur) {
+        int rc = build_graph(b);
+        if (rc != PLB_OK) return rc;
+    } else {
+        int rc = set_graph_grid(b);
+        if (rc != PLB_OK) return rc;
+    }
+    BCK(cudaEventRecord(b->ev0, b->st));
+    BCK(cudaGraphLaunch(b->gexec, b->st));
+    BCK(cudaEventRecord(b->ev1, b->st));
+    b->in_flight = true;
+    return PLB_OK;
+}
+
+int plb_batch_finish(plb_batch *b)
+{
+    if (!b) return PLB_ERR_ARG;
+    if (!b->in_flight) return PLB_OK;
+    BCK(cudaSetDevice(b->device));
+    BCK(cudaStreamSynchronize(b->st));
+    b->in_flight = false;
+    if (cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1) != cudaSuccess) b->last_ms = 0.f;
+    b->t += b->K;
+    /* K is even: the ping-pong parity is back where it started */
+    for (int sid = 0; sid < b->max_samples; sid++) {
+        SampleHost &h = b->s[sid];
+        if (!h.stepping) continue;
+        h.stepping = 0;
+        h.steps = b->t - h.start;
+        const double sux = b->h_ssum[3 * sid];
+        const double cells = (double)h.nx * h.ny * h.nz;
+        h.prev_ux = h.ux;
+        h.ux = sux / cells;
+        h.mass = b->h_ssum[3 * sid + 1];
+        h.k_darcy = h.force != 0.0 ? h.ux * h.nu / h.force : 0.0;
+        h.checks++;
+        const unsigned err = b->h_serr[sid];
+        if (err & 4u) { retire(b, sid, PLB_ERR_DENSITY); continue; }
+        if (err & 1u) { retire(b, sid, PLB_ERR_STATE); continue; }
+        const double change = fabs(h.ux - h.prev_ux);
+        if (h.checks >= 2 && h.ux != 0.0 && change <= h.tol * fabs(h.ux)) {
+            retire(b, sid, 1);
+            continue;
+        }
+        if (h.steps >= h.max_steps) { retire(b, sid, 2); continue; }
+        if (h.checks >= 2 && h.ux != 0.0 && h.handoff_tol > 0.0 &&
+            change <= h.handoff_tol * fabs(h.ux)) {
+            retire(b, sid, 4, true);
+            continue;
+        }
+        /* 16-bit deviations: keep the largest stored value near 2^13-2^14 */
+        if (b->precision == PLB_FP16DEV) {
+            const double big = b->h_ssum[3 * sid + 2];
+            float factor = 1.f;
+            if (big > 16384.0) factor = 0.25f;
+            else if (big > 0.0 && big < 2048.0 && h.scale < 1e9f) factor = 4.f;
+            if (factor != 1.f) {
+                const long long base = h.blk0 * B;
+                k_rescale<__half><<<gb(h.n, B), B, 0, b->st>>>((__half *)b->f[b->cur], b->npad,
+                                                              base, base + h.n, factor);
+                h.scale *= factor;
+                h.dev.co.scale = h.scale;
+                h.dev.co.inv_scale = 1.0f / h.scale;
+                BCK(cudaMemcpyAsync(b->sdev + sid, &h.dev, sizeof(SampleDev),
+                                    cudaMemcpyHostToDevice, b->st));
+            }
+        }
+    }
+    BCK(cudaStreamSynchronize(b->st));
+    return PLB_OK;
 }
 
 int plb_batch_run(plb_batch *b, int intervals, int *n_active)
 {
     if (!b || intervals < 0) return PLB_ERR_ARG;
-    BCK(cudaSetDevice(b->device));
     for (int r = 0; r < intervals; r++) {
         int act = 0;
-        for (auto &h : b->s) act += h.active;
+        int rc = plb_batch_launch(b, &act);
+        if (rc != PLB_OK) return rc;
         if (act == 0) break;
-        if (b->list_dirty) {
-            /* the pool blocks of the active samples, in pool order */
-            std::vector<std::pair<long long, int>> order;
-            for (int sid = 0; sid < b->max_samples; sid++)
-                if (b->s[sid].active) order.emplace_back(b->s[sid].blk0, sid);
-            std::sort(order.begin(), order.end());
-            b->hlist.clear();
-            for (auto &o : order) {
-                const SampleHost &h = b->s[o.second];
-                for (long long k = 0; k < h.nblk; k++) b->hlist.push_back((int)(h.blk0 + k));
-            }
-            if (!b->hlist.empty())
-                BCK(cudaMemcpyAsync(b->blist, b->hlist.data(), 4 * b->hlist.size(),
-                                    cudaMemcpyHostToDevice, b->st));
-            b->list_dirty = false;
-        }
-        if (!b->gexec || b->graph_n != (long long)b->hlist.size() || b->graph_cur != b->cur) {
-            int rc = build_graph(b);
-            if (rc != PLB_OK) return rc;
-        }
-        BCK(cudaGraphLaunch(b->gexec, b->st));
-        BCK(cudaStreamSynchronize(b->st));
-        b->t += b->K;
-        /* K is even: the ping-pong parity is back where it started */
-        for (int sid = 0; sid < b->max_samples; sid++) {
-            SampleHost &h = b->s[sid];
-            if (!h.active) continue;
-            h.steps = b->t - h.start;
-            const double sux = b->h_ssum[3 * sid];
-            const double cells = (double)h.nx * h.ny * h.nz;
-            h.prev_ux = h.ux;
-            h.ux = sux / cells;
-            h.mass = b->h_ssum[3 * sid + 1];
-            h.k_darcy = h.force != 0.0 ? h.ux * h.nu / h.force : 0.0;
-            h.checks++;
-            const unsigned err = b->h_serr[sid];
-            if (err & 4u) { retire(b, sid, PLB_ERR_DENSITY); continue; }
-            if (err & 1u) { retire(b, sid, PLB_ERR_STATE); continue; }
-            if (h.checks >= 2 && h.ux != 0.0 &&
-                fabs(h.ux - h.prev_ux) <= h.tol * fabs(h.ux)) {
-                retire(b, sid, 1);
-                continue;
-            }
-            if (h.steps >= h.max_steps) { retire(b, sid, 2); continue; }
-            /* 16-bit deviations: keep the largest stored value near 2^13-2^14 */
-            if (b->precision == PLB_FP16DEV) {
-                const double big = b->h_ssum[3 * sid + 2];
-                float factor = 1.f;
-                if (big > 16384.0) factor = 0.25f;
-                else if (big > 0.0 && big < 2048.0 && h.scale < 1e9f) factor = 4.f;
-                if (factor != 1.f) {
-                    const long long base = h.blk0 * B;
-                    k_rescale<__half><<<gb(h.n, B), B, 0, b->st>>>((__half *)b->f[b->cur], b->npad,
-                                                                  base, base + h.n, factor);
-                    h.scale *= factor;
-                    h.dev.co.scale = h.scale;
-                    h.dev.co.inv_scale = 1.0f / h.scale;
-                    BCK(cudaMemcpyAsync(b->sdev + sid, &h.dev, sizeof(SampleDev),
-                                        cudaMemcpyHostToDevice, b->st));
-                    BCK(cudaStreamSynchronize(b->st));
-                }
-            }
-        }
-        BCK(cudaStreamSynchronize(b->st));
+        rc = plb_batch_finish(b);
+        if (rc != PLB_OK) return rc;
     }
     if (n_active) {
         int act = 0;
         for (auto &h : b->s) act += h.active;
         *n_active = act;
     }
+    return PLB_OK;
+}
+
+static bool dev_form(int precision)
+{
+    return precision == PLB_FP32 || precision == PLB_FP16DEV || precision == PLB_BF16DEV;
+}
+
+template <typename TI>
+static void convert_to(const plb_batch *src, const SampleHost &hs, plb_batch *dst,
+                       long long db, float scale_out)
+{
+    const TI *in = (const TI *)src->f[src->cur];
+    const long long sb = hs.blk0 * B;
+    const float inv = 1.0f / hs.scale;
+    switch (dst->precision) {
+    case PLB_FP32:
+        k_convert_dev<TI, float><<<gb(hs.n, B), B, 0, dst->adm>>>(
+            in, src->npad, sb, inv, (float *)dst->f[dst->cur], dst->npad, db, scale_out, hs.n);
+        break;
+    case PLB_FP16DEV:
+        k_convert_dev<TI, __half><<<gb(hs.n, B), B, 0, dst->adm>>>(
+            in, src->npad, sb, inv, (__half *)dst->f[dst->cur], dst->npad, db, scale_out, hs.n);
+        break;
+    default:
+        k_convert_dev<TI, __nv_bfloat16><<<gb(hs.n, B), B, 0, dst->adm>>>(
+            in, src->npad, sb, inv, (__nv_bfloat16 *)dst->f[dst->cur], dst->npad, db,
+            scale_out, hs.n);
+        break;
+    }
+}
+
+int plb_batch_transfer(plb_batch *src, int id, plb_batch *dst, int *new_id)
+{
+    if (!src || !dst || src == dst || !new_id || id < 0 || id >= src->max_samples)
+        return PLB_ERR_ARG;
+    const SampleHost &hs = src->s[id];
+    if (!hs.used || !hs.parked) return PLB_ERR_STATE;
+    if (src->device != dst->device || src->K != dst->K || !dev_form(src->precision) ||
+        !dev_form(dst->precision))
+        return PLB_ERR_ARG;
+    BCK(cudaSetDevice(dst->device));
+    int sid = -1;
+    for (int k = 0; k < dst->max_samples; k++)
+        if (!dst->s[k].used) { sid = k; break; }
+    if (sid < 0) return PLB_ERR_NOMEM;
+    const long long blk0 = alloc_blocks(dst, hs.nblk);
+    if (blk0 < 0) return PLB_ERR_NOMEM;
+    const long long sb = hs.blk0 * B, db = blk0 * B;
+    const int n = hs.n;
+    /* the 16-bit target keeps the source's scale, or takes one that puts
+     * the largest deviation near 2^13 */
+    float scale = 1.f;
+    if (dst->precision == PLB_FP16DEV) {
+        if (src->precision == PLB_FP16DEV) {
+            scale = hs.scale;
+        } else {
+            double g = 3.0 * fabs(hs.force) * dst->K;
+            if (g < 1e-6) g = 1e-6;
+            scale = (float)exp2(floor(log2(8192.0 / g)));
+            if (scale > 1e9f) scale = 1e9f;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (n > 0) {
+        e = cudaMemcpyAsync(dst->perm + db, src->perm + sb, 4 * (size_t)n,
+                            cudaMemcpyDeviceToDevice, dst->adm);
+        for (int r = 0; r < 3 && e == cudaSuccess; r++)
+            e = cudaMemcpyAsync(dst->coord + r * dst->npad + db, src->coord + r * src->npad + sb,
+                                2 * (size_t)n, cudaMemcpyDeviceToDevice, dst->adm);
+        if (e == cudaSuccess) {
+            k_translate_words<<<gb(n, B), B, 0, dst->adm>>>(src->nbr, src->npad, sb,
+                                                           (uint32_t)src->rest, dst->nbr,
+                                                           dst->npad, db, (uint32_t)dst->rest, n);
+            switch (src->precision) {
+            case PLB_FP32: convert_to<float>(src, hs, dst, db, scale); break;
+            case PLB_FP16DEV: convert_to<__half>(src, hs, dst, db, scale); break;
+            default: convert_to<__nv_bfloat16>(src, hs, dst, db, scale); break;
+            }
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) {
+        free_range(dst, blk0, hs.nblk);
+        fprintf(stderr, "porelb_gpu: batch transfer failed: %s\n", cudaGetErrorString(e));
+        return PLB_ERR_CUDA;
+    }
+    SampleHost &h = dst->s[sid];
+    h = hs;
+    h.used = 1;
+    h.active = 0;
+    h.finished = 0;
+    h.parked = 0;
+    h.stepping = 0;
+    h.pending = 0;
+    h.status = 0;
+    h.handoff_tol = 0.0;
+    h.blk0 = blk0;
+    h.scale = scale;
+    /* the step count goes on from where the source pool stopped (the
+     * it > 0 rule of porelb.c:347-348 counts from the sample's start) */
+    h.start = dst->t + (dst->in_flight ? dst->K : 0) - hs.steps;
+    SampleDev &d = h.dev;
+    memset(&d, 0, sizeof(d));
+    make_coeffs(h.tau, h.force, h.scale, &d.co);
+    d.base = db;
+    d.n = n;
+    d.start = (int)h.start;
+    BCK(cudaMemcpyAsync(dst->sdev + sid, &d, sizeof(d), cudaMemcpyHostToDevice, dst->adm));
+    BCK(cudaMemsetAsync(dst->serr + sid, 0, 4, dst->adm));
+    k_set_blocks<<<gb(hs.nblk, B), B, 0, dst->adm>>>(dst->blk, blk0, hs.nblk, sid, n);
+    BCK(cudaGetLastError());
+    BCK(cudaStreamSynchronize(dst->adm));
+    activate(dst, sid);
+    *new_id = sid;
     return PLB_OK;
 }
 
@@ -682,8 +987,18 @@ int plb_batch_result(plb_batch *b, int id, double *k_darcy, double *mean_ux,
 int plb_batch_release(plb_batch *b, int id)
 {
     if (!b || id < 0 || id >= b->max_samples || !b->s[id].used) return PLB_ERR_ARG;
+    /* a sample the interval in flight steps is released after it */
+    if (b->s[id].stepping) return PLB_ERR_STATE;
     BCK(cudaSetDevice(b->device));
     if (b->s[id].active) retire(b, id, 3);
+    if (b->s[id].parked) {
+        SampleHost &h = b->s[id];
+        k_set_blocks<<<gb(h.nblk, B), B, 0, b->adm>>>(b->blk, h.blk0, h.nblk, -1, 0);
+        BCK(cudaGetLastError());
+        BCK(cudaStreamSynchronize(b->adm));
+        free_range(b, h.blk0, h.nblk);
+        h.parked = 0;
+    }
     BCK(cudaStreamSynchronize(b->st));
     for (auto it = b->done.begin(); it != b->done.end();)
         it = (*it == id) ? b->done.erase(it) : std::next(it);
@@ -693,8 +1008,10 @@ int plb_batch_release(plb_batch *b, int id)
 
 int plb_batch_get_f(plb_batch *b, int id, double *f_aos)
 {
-    if (!b || id < 0 || id >= b->max_samples || !b->s[id].active || !f_aos)
+    if (!b || id < 0 || id >= b->max_samples || !(b->s[id].active || b->s[id].parked) ||
+        !f_aos)
         return PLB_ERR_ARG;
+    if (b->in_flight) return PLB_ERR_STATE;
     BCK(cudaSetDevice(b->device));
     const SampleHost &h = b->s[id];
     if (h.n == 0) return PLB_OK;
@@ -725,6 +1042,7 @@ int plb_batch_get_macros(plb_batch *b, int id, double *rho, double *ux,
 {
     if (!b || id < 0 || id >= b->max_samples || !b->s[id].active || !b->macro)
         return PLB_ERR_ARG;
+    if (b->in_flight) return PLB_ERR_STATE;
     BCK(cudaSetDevice(b->device));
     const SampleHost &h = b->s[id];
     if (h.n == 0) return PLB_OK;
@@ -774,6 +1092,13 @@ int plb_batch_free_nodes(plb_batch *b, long long *largest_range, long long *tota
     for (const auto &h : b->s) slots += !h.used;
     if (largest_range) *largest_range = slots > 0 ? big * B : 0;
     if (total) *total = all * B;
+    return PLB_OK;
+}
+
+int plb_batch_interval_ms(plb_batch *b, float *ms)
+{
+    if (!b || !ms) return PLB_ERR_ARG;
+    *ms = b->last_ms;
     return PLB_OK;
 }
 

@@ -97,7 +97,8 @@ struct BatchArgs {
     void *fout;
     const uint32_t *nbr;
     long long npad;
-    const int *blk_list;       /* pool blocks this launch covers (one CTA each) */
+    const int *blk_list;       /* pool blocks this launch covers (one CTA each,
+                                  two for 128-thread CTAs) */
     const int *blk_sample;     /* per 256-node pool block: sample << 9 | nodes of
                                   the sample in the block, -1 = free */
     long long part_stride;     /* pool blocks: stride of the partial-sum rows */
@@ -138,10 +139,11 @@ int batch_ctas_per_block(int precision);
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
                         int block, int variant, cudaStream_t s);
 
-/* One step of every active block of a batch pool (256 nodes per block). */
+/* The batch step kernel (one BatchArgs argument) of a storage form, for a
+ * graph kernel node; *cta_threads receives its CTA size (pool blocks of
+ * 256 nodes, 256 / CTA size CTAs each). */
 constexpr int kBatchBlock = 256;
-cudaError_t launch_batch_step(int precision, bool macros, const BatchArgs &a,
-                              int nblocks, cudaStream_t s);
+const void *batch_step_kernel(int precision, bool macros, int *cta_threads);
 
 /* Fill the coefficients from tau, F and the storage scale. */
 void make_coeffs(double tau, double force, float scale, Coeffs *c);

@@ -1,29 +1,34 @@
 """Permeability-solve server with continuous batching.
 
 Requests (geometry seed and size, porosity, sphere radius, tau, force,
-tolerance) arrive over time.  The server keeps one device node pool (a
-``Batch``) sized from an HBM budget; at every interval boundary it admits
-waiting requests that fit (first come first served, with smaller requests
-allowed to pass a head that does not fit), builds their geometry and node
-table on the device, advances every resident sample by one interval (K
-lattice steps in one CUDA-graph replay), and retires converged samples,
-whose blocks the next admissions reuse.  Work of requests that arrived while
-others run overlaps on the device with theirs.
+tolerance) arrive over time.  The server keeps device node pools
+(``Batch``) sized from an HBM budget.  Each round it launches one interval
+(K lattice steps, one CUDA-graph replay) on every pool that has work and,
+while those run, admits waiting requests that fit (first come first served,
+smaller requests may pass a head that does not fit): their geometry and node
+table are built on the pool's admission stream, concurrently with the
+interval, and they join at the next launch.  Then it waits for the
+intervals, answers converged requests and backfills their blocks.  Work of
+requests that arrive while others run overlaps on the device with theirs.
+
+Storage forms:
+* one pool in FP32 (default), FP64, FP16 or BF16 deviations;
+* ``"fp16dev"`` with ``handoff_tol``: requests start in a pool of scaled
+  FP16 deviations (148 B per lattice update against FP32's 224) and, once
+  the relative change of <u_x> over an interval falls below handoff_tol,
+  move with their state and history into an FP32 pool, where the
+  steady-state test finishes at the request's own tolerance.  FP16
+  storage alone cannot finish at tight tolerances: once a sample is
+  steady, its <u_x> keeps wandering by 2e-7 to 5e-7 of itself from check
+  to check (FP32: below 4e-9), so a 1e-7 test passes only by chance.
 
 Latency of a request = completion time - arrival time (wall clock).
-
-The pool's storage form defaults to FP32.  Once a sample is steady, the
-16-bit forms keep <u_x> fluctuating by about 1e-7 to 2e-6 of itself from
-one check to the next (FP32: below 4e-9), so a steady-state test tighter
-than that passes only by chance and such requests run several times longer
-in FP16 than in FP32.
 """
 import time
 
 import numpy as np
 
-from .batch import Batch
-
+from .batch import PARKED, Batch
 
 # a request whose estimated fluid nodes exceed the free room by more than
 # this factor is not tried: the generator stops at or just below the target
@@ -39,16 +44,27 @@ def _blocks_nodes(n):
 
 class Server:
     def __init__(self, hbm_budget_bytes, precision="fp32", check_every=500,
-                 max_samples=4096, device=0, lookahead=64, batch=None):
-        if batch is None:
-            bpn = Batch.bytes_per_node(precision)
-            self.capacity = int(hbm_budget_bytes // bpn)
-            batch = Batch(self.capacity, max_samples, precision, check_every,
-                          device=device)
-        self.batch = batch
-        self.capacity = int(batch.info()["capacity_nodes"])
+                 max_samples=4096, device=0, lookahead=64, batch=None,
+                 handoff_tol=None, handoff_share=0.35):
+        """precision: the storage form requests start in.  handoff_tol (only
+        with "fp16dev"; default 1e-5): move a request to an FP32 pool once
+        its relative change is below it; handoff_share: the FP32 pool's
+        share of the budget.  batch: a ready pool (tests)."""
         self.precision = precision
         self.lookahead = lookahead
+        if precision == "fp16dev" and handoff_tol is None:
+            handoff_tol = 1e-5
+        self.handoff_tol = handoff_tol if precision == "fp16dev" else None
+        self.tail = None
+        if batch is None:
+            share = handoff_share if self.handoff_tol else 0.0
+            cap = int(hbm_budget_bytes * (1 - share) // Batch.bytes_per_node(precision))
+            batch = Batch(cap, max_samples, precision, check_every, device=device)
+            if self.handoff_tol:
+                cap32 = int(hbm_budget_bytes * share // Batch.bytes_per_node("fp32"))
+                self.tail = Batch(cap32, max_samples, "fp32", check_every, device=device)
+        self.batch = batch
+        self.capacity = int(batch.info()["capacity_nodes"])
 
     @staticmethod
     def estimated_nodes(r):
@@ -58,6 +74,22 @@ class Server:
 
     def close(self):
         self.batch.close()
+        if self.tail is not None:
+            self.tail.close()
+
+    def pools(self):
+        return [self.batch] + ([self.tail] if self.tail is not None else [])
+
+    def _answer(self, done, v, res, t0, time_scale, status=None, handed_off=False):
+        end = time.perf_counter() - t0
+        r = v["req"]
+        done.append(dict(index=r.index, edge=r.edge, nodes=v["nodes"],
+                         arrival=r.arrival * time_scale, admitted=v["admitted"],
+                         finished=end, latency=end - r.arrival * time_scale,
+                         steps=res["steps"], k_darcy=res["k_darcy"],
+                         status=res["status"] if status is None else status,
+                         tau=r.tau, tol=r.tol, handed_off=handed_off,
+                         handoff_steps=v.get("handoff_steps")))
 
     def serve(self, requests, time_scale=1.0, max_wall=None):
         """Serve requests (objects with .arrival in seconds, .edge, .seed,
@@ -65,25 +97,32 @@ class Server:
         list of per-request records and a summary."""
         pending = sorted(requests, key=lambda r: r.arrival)
         waiting = []
-        live = {}
+        live = {}        # (pool index, sid) -> record
+        parked = []      # sids parked in the first pool, waiting for room
         done = []
         rejected = []
         t0 = time.perf_counter()
         node_steps = 0
-        intervals = 0
-        t_admit = t_run = 0.0
+        rounds = 0
+        t_admit = t_wait = busy_ms = 0.0
+        handoffs = 0
+        pools = self.pools()
         K = self.batch.check_every
+        head = self.batch
         while pending or waiting or live:
             now = time.perf_counter() - t0
             if max_wall is not None and now > max_wall:
                 break
             while pending and pending[0].arrival * time_scale <= now:
                 waiting.append(pending.pop(0))
-            # admission: FCFS with bounded lookahead past a head that does
-            # not fit into the free node ranges
-            admitted = []
+            # one interval on every pool with work, asynchronously
+            stepping = [p.launch() for p in pools]
+            node_steps += sum(v["nodes"] for (pi, _), v in live.items()
+                              if stepping[pi] and not v.get("parked")) * K
+            # admissions while the intervals run
             ta = time.perf_counter()
-            room = self.batch.free_nodes()[0]
+            admitted = []
+            room = head.free_nodes()[0]
             for r in waiting[: self.lookahead]:
                 est = _EST_SLACK * self.estimated_nodes(r)
                 if est > self.capacity:
@@ -93,45 +132,68 @@ class Server:
                     continue
                 if live and _blocks_nodes(est) > room:
                     continue  # no room now: skip building its geometry
-                sid = self.batch.try_add_packed(
+                sid = head.try_add_packed(
                     r.seed, r.edge, r.edge, r.edge, r.rmin, r.rmax, r.porosity,
-                    r.tau, r.force, tol=r.tol)
+                    r.tau, r.force, tol=r.tol,
+                    handoff_tol=self.handoff_tol or 0.0)
                 if sid is not None:
-                    live[sid] = dict(req=r, admitted=time.perf_counter() - t0,
-                                     nodes=self.batch.num_nodes(sid))
+                    live[(0, sid)] = dict(req=r, admitted=time.perf_counter() - t0,
+                                          nodes=head.num_nodes(sid))
                     admitted.append(r)
-                    room = self.batch.free_nodes()[0]
-                elif not live:
+                    room = head.free_nodes()[0]
+                elif not live and not any(stepping):
                     # it did not fit into the empty pool: it never will
                     rejected.append(self._reject(r, t0, time_scale))
                     admitted.append(r)
                 else:
-                    room = self.batch.free_nodes()[0]
+                    room = head.free_nodes()[0]
             for r in admitted:
                 waiting.remove(r)
             t_admit += time.perf_counter() - ta
-            if not live:
-                if pending:
+            if not any(stepping):
+                if not live and pending:
                     time.sleep(max(0.0, pending[0].arrival * time_scale -
                                    (time.perf_counter() - t0)))
-                continue
-            node_steps += sum(v["nodes"] for v in live.values()) * K
-            tr = time.perf_counter()
-            self.batch.run(1)
-            t_run += time.perf_counter() - tr
-            intervals += 1
-            for sid in self.batch.poll():
-                res = self.batch.result(sid)
-                v = live.pop(sid)
-                end = time.perf_counter() - t0
-                r = v["req"]
-                done.append(dict(index=r.index, edge=r.edge, nodes=v["nodes"],
-                                 arrival=r.arrival * time_scale,
-                                 admitted=v["admitted"], finished=end,
-                                 latency=end - r.arrival * time_scale,
-                                 steps=res["steps"], k_darcy=res["k_darcy"],
-                                 status=res["status"], tau=r.tau, tol=r.tol))
+                if not parked:
+                    continue
+            tw = time.perf_counter()
+            for p in pools:
+                p.finish()
+            t_wait += time.perf_counter() - tw
+            busy_ms += max(p.interval_ms() if s else 0.0 for p, s in zip(pools, stepping))
+            rounds += 1
+            for pi, p in enumerate(pools):
+                for sid in p.poll():
+                    res = p.result(sid)
+                    if res["status"] == PARKED:
+                        live[(pi, sid)]["parked"] = True
+                        live[(pi, sid)]["handoff_steps"] = res["steps"]
+                        parked.append(sid)
+                        continue
+                    self._answer(done, live.pop((pi, sid)), res, t0, time_scale,
+                                 handed_off=pi == 1)
+                    p.release(sid)
+            # parked 16-bit samples move to the FP32 pool when it has room
+            still = []
+            tail_busy = any(pi == 1 for pi, _ in live)
+            for sid in parked:
+                nid = self.batch.try_transfer(sid, self.tail)
+                if nid is None and not tail_busy:
+                    # larger than the whole FP32 pool: answered at the
+                    # handoff tolerance, marked as such (PLB_ERR_NOMEM)
+                    self._answer(done, live.pop((0, sid)), self.batch.result(sid), t0,
+                                 time_scale, status=-5)
+                    self.batch.release(sid)
+                    continue
+                if nid is None:
+                    still.append(sid)
+                    continue
+                v = live.pop((0, sid))
+                v.pop("parked", None)
+                live[(1, nid)] = v
                 self.batch.release(sid)
+                handoffs += 1
+            parked = still
         wall = time.perf_counter() - t0
         lat = np.array([d["latency"] for d in done]) if done else np.zeros(1)
         summary = dict(requests=len(done), wall_s=wall,
@@ -139,8 +201,11 @@ class Server:
                        p50_latency_s=float(np.percentile(lat, 50)),
                        p99_latency_s=float(np.percentile(lat, 99)),
                        fluid_mlups=node_steps / wall / 1e6 if wall > 0 else 0.0,
-                       intervals=intervals, capacity_nodes=self.capacity,
-                       admit_s=t_admit, run_s=t_run,
+                       intervals=rounds, capacity_nodes=self.capacity,
+                       admit_s=t_admit, wait_s=t_wait,
+                       gpu_busy_s=busy_ms / 1e3,
+                       gpu_idle_frac=max(0.0, 1.0 - busy_ms / 1e3 / wall) if wall > 0 else None,
+                       handoffs=handoffs, handoff_tol=self.handoff_tol,
                        precision=self.precision, check_every=K,
                        rejected=[d["index"] for d in rejected])
         return done, summary

@@ -25,7 +25,8 @@ class FakePool:
         free = self.cap - self.used
         return free, free
 
-    def try_add_packed(self, seed, nx, ny, nz, rmin, rmax, phi, tau, force, tol):
+    def try_add_packed(self, seed, nx, ny, nz, rmin, rmax, phi, tau, force, tol,
+                       handoff_tol=0.0):
         self.adds += 1
         n = int(nx * ny * nz * phi)
         if n > self.cap - self.used:
@@ -39,11 +40,20 @@ class FakePool:
     def num_nodes(self, sid):
         return self.live[sid][0]
 
-    def run(self, k):
-        for sid, v in list(self.live.items()):
+    def launch(self):
+        self.stepping = [sid for sid, v in self.live.items() if v[1] > 0]
+        return len(self.stepping)
+
+    def finish(self):
+        for sid in getattr(self, "stepping", []):
+            v = self.live[sid]
             v[1] -= 1
             if v[1] == 0:
                 self.finished.append(sid)
+        self.stepping = []
+
+    def interval_ms(self):
+        return 0.0
 
     def poll(self):
         out, self.finished = self.finished, []
