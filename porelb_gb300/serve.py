@@ -43,7 +43,7 @@ def _blocks_nodes(n):
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes, precision="fp32", check_every=500,
+    def __init__(self, hbm_budget_bytes, precision="fp32", check_every=250,
                  max_samples=4096, device=0, lookahead=64, batch=None,
                  handoff_tol=None, handoff_share=0.35):
         """precision: the storage form requests start in.  handoff_tol (only
