@@ -545,7 +545,11 @@ def batched_result(n_samples, K, max_steps, plain_steps):
     import torch
     import porelb_gb300 as P
     from porelb_gb300.workloads import batched_samples
+    from porelb_gb300 import tune
     samples = batched_samples(n_samples, 3)
+    # the pools take the launch tuner's choice for their form
+    launch = {f: {k: v for k, v in tune.ensure_pool(f).items() if k != "tune_s"}
+              for f in ("fp32", "fp64")}
     res32, ns32, wall32 = _steady_batch(samples, "fp32", K, max_steps)
     res64, ns64, wall64 = _steady_batch(samples, "fp64", K, max_steps)
     # plain kernel per sample (FP32), timed on a fixed step count, then the
@@ -578,6 +582,7 @@ def batched_result(n_samples, K, max_steps, plain_steps):
                               "within_1e-3": sum(e <= 1e-3 for e in errs),
                               "of": len(errs)},
         "wall_s": round(wall32, 2), "check_every": K,
+        "pool_launch_tuned": launch,
         "config": {"workload": f"batched {len(samples)} samples, seed 3",
                    "edges": [s.edge for s in samples],
                    "tol": 1e-7, "force": 1e-6, "max_steps": max_steps},
@@ -684,6 +689,7 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
         "gpu_idle_frac": (round(summ["gpu_idle_frac"], 4)
                           if summ["gpu_idle_frac"] is not None else None),
         "handoffs": summ["handoffs"], "handoff_tol": summ["handoff_tol"],
+        "pool_launch_tuned": summ["pool_launch"],
         "config": {"workload": f"{len(reqs)} Poisson requests, seed 4",
                    "rate_per_s": rate, "budget_gb": budget_gb,
                    "check_every": K, "storage": precision,

@@ -275,6 +275,23 @@ size_t plb_batch_bytes_per_node(int precision, int keep_macros);
 int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
                      int check_every, int keep_macros, int device,
                      plb_batch **out);
+/* Pool parameters with the launch choices the tuner makes (zero = the
+ * library default for each choice). */
+typedef struct {
+    size_t capacity_nodes; /* pool size */
+    int max_samples;
+    int precision;         /* PLB_FP64 ... */
+    int check_every;       /* interval K (even) */
+    int keep_macros;
+    int device;
+    int cta_threads;       /* batch-step CTA: 128 or 256 threads (0: 128 for
+                              PLB_FP64, 256 otherwise) */
+    int l2_prefetch;       /* L2 prefetch of the pool block half a wave
+                              ahead: 0 = default (on for PLB_FP64), 1 on,
+                              -1 off */
+    int reserved[6];
+} plb_batch_params;
+int plb_batch_create_ex(const plb_batch_params *p, plb_batch **out);
 void plb_batch_destroy(plb_batch *b);
 /* Admit a sample from a host flag grid (0/1) or a device sphere pack.
  * PLB_ERR_NOMEM when no free range or sample slot is left. */

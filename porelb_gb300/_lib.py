@@ -49,6 +49,14 @@ class SampleParams(ctypes.Structure):
                 ("handoff_tol", ctypes.c_double), ("reserved", ctypes.c_int * 2)]
 
 
+class BatchParams(ctypes.Structure):
+    _fields_ = [("capacity_nodes", ctypes.c_size_t), ("max_samples", ctypes.c_int),
+                ("precision", ctypes.c_int), ("check_every", ctypes.c_int),
+                ("keep_macros", ctypes.c_int), ("device", ctypes.c_int),
+                ("cta_threads", ctypes.c_int), ("l2_prefetch", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -97,6 +105,7 @@ _SIGS = {
     "plb_batch_add_packed": (_I, [_P, ctypes.c_uint64, _I, _I, _I, _D, _D, _D,
                                   ctypes.POINTER(SampleParams), _IP, _IP,
                                   _DP]),
+    "plb_batch_create_ex": (_I, [ctypes.POINTER(BatchParams), ctypes.POINTER(_P)]),
     "plb_batch_run": (_I, [_P, _I, _IP]),
     "plb_batch_launch": (_I, [_P, _IP]),
     "plb_batch_finish": (_I, [_P]),

@@ -140,6 +140,12 @@ def _params(tau, force, precision, ordering, halo, block_size, device,
     return p
 
 
+def _tuned(precision, n, boundary):
+    from . import tune
+    c = tune.best(precision, n, boundary)
+    return c["block_size"], c["ordering"], c["kernel_variant"]
+
+
 # ------------------------------------------------------------------ solver
 
 class Simulation:
@@ -148,9 +154,13 @@ class Simulation:
     def __init__(self, V, nx, ny, nz, v_sub_start=None, tau=0.8,
                  force=1e-3, precision="fp64_exact", ordering="morton",
                  halo="auto", block_size=0, device=0, boundary="reference",
-                 kernel_variant=0, prefetch=None):
+                 kernel_variant=0, prefetch=None, tuned=False):
+        """tuned: take block size, ordering and register budget from the
+        launch tuner's cached choice for this form and size (tune.tune)."""
         self._lib = _lib.load()
         self.V = np.ascontiguousarray(V, dtype=NODE_DTYPE)
+        if tuned:
+            block_size, ordering, kernel_variant = _tuned(precision, len(self.V), boundary)
         self.nx, self.ny, self.nz = nx, ny, nz
         vs = np.zeros(1, np.int32) if v_sub_start is None else v_sub_start
         self.v_sub_start = np.ascontiguousarray(vs, dtype=np.int32)
@@ -280,12 +290,15 @@ class Simulation:
     def from_flag(cls, flag, nx, ny, nz, num_p=1, tau=0.8, force=1e-3,
                   precision="fp64_exact", ordering="morton", halo="auto",
                   block_size=0, device=0, boundary="reference",
-                  kernel_variant=0, prefetch=None):
+                  kernel_variant=0, prefetch=None, tuned=False):
         """build_V + create on the device from a 0/1 flag grid."""
         lib = _lib.load()
         flag = np.ascontiguousarray(flag, dtype=np.uint8).reshape(-1)
         if flag.size != nx * ny * nz:
             raise ValueError("flag size does not match nx*ny*nz")
+        if tuned:
+            block_size, ordering, kernel_variant = _tuned(
+                precision, int(np.count_nonzero(flag == 1)), boundary)
         p = _params(tau, force, precision, ordering, halo, block_size, device,
                     boundary, kernel_variant, prefetch)
         h = ctypes.c_void_p()

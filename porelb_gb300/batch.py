@@ -20,16 +20,35 @@ PARKED = 4
 
 class Batch:
     def __init__(self, capacity_nodes, max_samples=1024, precision="fp32",
-                 check_every=1000, keep_macros=False, device=0):
+                 check_every=1000, keep_macros=False, device=0, cta_threads=None,
+                 l2_prefetch=None):
+        """cta_threads (128 or 256) and l2_prefetch (True/False): the batch
+        step's launch; None takes the launch tuner's cached choice for this
+        form (porelb_gb300.tune.tune_pool), else the library default."""
         self._lib = _lib.load()
         self.precision = precision
         self.check_every = check_every
+        if cta_threads is None or l2_prefetch is None:
+            from . import tune
+            choice = tune.best_pool(precision)
+            if cta_threads is None:
+                cta_threads = choice["cta_threads"]
+            if l2_prefetch is None:
+                l2_prefetch = choice["l2_prefetch"]
+        bp = _lib.BatchParams()
+        bp.capacity_nodes = int(capacity_nodes)
+        bp.max_samples = max_samples
+        bp.precision = PRECISIONS[precision]
+        bp.check_every = check_every
+        bp.keep_macros = int(keep_macros)
+        bp.device = device
+        bp.cta_threads = int(cta_threads or 0)
+        bp.l2_prefetch = 0 if l2_prefetch is None else (1 if l2_prefetch else -1)
         h = ctypes.c_void_p()
-        _check(self._lib.plb_batch_create(int(capacity_nodes), max_samples,
-                                          PRECISIONS[precision], check_every,
-                                          int(keep_macros), device,
-                                          ctypes.byref(h)), "plb_batch_create")
+        _check(self._lib.plb_batch_create_ex(ctypes.byref(bp), ctypes.byref(h)),
+               "plb_batch_create_ex")
         self._h = h
+        self.launch_choice = dict(cta_threads=cta_threads, l2_prefetch=l2_prefetch)
         self.meta = {}
 
     @staticmethod

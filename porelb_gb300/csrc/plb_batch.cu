@@ -250,6 +250,8 @@ struct plb_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr; /* around the interval in flight */
     float last_ms = 0.f;
     bool in_flight = false;
+    int cta = 256;     /* threads per CTA of the batch step */
+    int prefetch = 0;  /* L2 prefetch of the pool block half a wave ahead */
     long long cap_blocks = 0, npad = 0, rest = 0;
     void *f[2] = {nullptr, nullptr};
     int cur = 0;
@@ -341,8 +343,28 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
                      int check_every, int keep_macros, int device,
                      plb_batch **out)
 {
-    if (!out) return PLB_ERR_ARG;
+    plb_batch_params bp;
+    memset(&bp, 0, sizeof(bp));
+    bp.capacity_nodes = capacity_nodes;
+    bp.max_samples = max_samples;
+    bp.precision = precision;
+    bp.check_every = check_every;
+    bp.keep_macros = keep_macros;
+    bp.device = device;
+    return plb_batch_create_ex(&bp, out);
+}
+
+int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
+{
+    if (!out || !bp) return PLB_ERR_ARG;
     *out = nullptr;
+    const size_t capacity_nodes = bp->capacity_nodes;
+    const int max_samples = bp->max_samples, precision = bp->precision;
+    const int check_every = bp->check_every, keep_macros = bp->keep_macros;
+    const int device = bp->device;
+    if ((bp->cta_threads != 0 && bp->cta_threads != 128 && bp->cta_threads != B) ||
+        bp->l2_prefetch < -1 || bp->l2_prefetch > 1)
+        return PLB_ERR_ARG;
     if (capacity_nodes == 0 || max_samples <= 0 || max_samples > (1 << 22) ||
         elem_of(precision) == 0 ||
         check_every <= 0 || (check_every & 1) || capacity_nodes >= (size_t)kMaxNodes - B)
@@ -358,6 +380,8 @@ int plb_batch_create(size_t capacity_nodes, int max_samples, int precision,
     b->keep_macros = keep_macros;
     b->max_samples = max_samples;
     b->elem = elem_of(precision);
+    b->cta = bp->cta_threads ? bp->cta_threads : batch_default_cta(precision);
+    b->prefetch = bp->l2_prefetch > 0 || (bp->l2_prefetch == 0 && precision == PLB_FP64);
     b->cap_blocks = (long long)((capacity_nodes + B - 1) / B);
     b->rest = b->cap_blocks * B;
     b->npad = b->rest + B;
@@ -587,9 +611,9 @@ static int build_graph(plb_batch *b)
     a.nbr = b->nbr;
     a.npad = b->npad;
     a.blk_list = b->blist;
-    /* the FP64 form prefetches the pool block half a wave of CTAs ahead */
-    a.pf_blocks = b->precision == PLB_FP64 ? (batch_wave_blocks(b->precision) + 1) / 2 : 0;
-    const int h = batch_ctas_per_block(b->precision);
+    /* prefetch the pool block half a wave of CTAs ahead (FP64 by default) */
+    a.pf_blocks = b->prefetch ? (batch_wave_blocks(b->precision, b->cta) + 1) / 2 : 0;
+    const int h = B / b->cta;
     a.part_stride = h * b->cap_blocks;
     a.blk_sample = b->blk;
     a.samples = b->sdev;
@@ -597,9 +621,9 @@ static int build_graph(plb_batch *b)
     a.macro = b->macro;
     a.partial = b->partial;
     a.serr = b->serr;
-    int bt = 0;
-    const void *fn = batch_step_kernel(b->precision, false, &bt);
-    const void *fn_m = batch_step_kernel(b->precision, true, &bt);
+    const int bt = b->cta;
+    const void *fn = batch_step_kernel(b->precision, false, bt);
+    const void *fn_m = batch_step_kernel(b->precision, true, bt);
     b->step_args.assign((size_t)b->K, a);
     b->step_nodes.assign((size_t)b->K, nullptr);
     b->graph_grid = (int)b->hlist.size() * h;
@@ -679,12 +703,12 @@ static int build_graph(plb_batch *b)
  * count as their grid. */
 static int set_graph_grid(plb_batch *b)
 {
-    const int h = batch_ctas_per_block(b->precision);
+    const int h = B / b->cta;
     const int grid = (int)b->hlist.size() * h;
     if (grid == b->graph_grid || grid == 0) return PLB_OK;
-    int bt = 0;
-    const void *fn = batch_step_kernel(b->precision, false, &bt);
-    const void *fn_m = batch_step_kernel(b->precision, true, &bt);
+    const int bt = b->cta;
+    const void *fn = batch_step_kernel(b->precision, false, bt);
+    const void *fn_m = batch_step_kernel(b->precision, true, bt);
     for (int k = 0; k < b->K; k++) {
         void *kp[1] = {&b->step_args[(size_t)k]};
         cudaKernelNodeParams p;

@@ -131,19 +131,18 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
 /* Launch one step of the given precision. */
 /* blocks of the step kernel resident on the device at once (0 if unknown) */
 int step_wave_blocks(int precision, int block, int variant);
-/* the same for the batch step kernel */
-int batch_wave_blocks(int precision);
-/* CTAs of the batch step per 256-node pool block (partial-sum rows per
- * pool block) */
-int batch_ctas_per_block(int precision);
+/* the same for the batch step kernel with CTAs of `cta` threads */
+int batch_wave_blocks(int precision, int cta);
+/* default threads per CTA of the batch step (128 or 256) */
+int batch_default_cta(int precision);
 cudaError_t launch_step(int precision, bool macros, const StepArgs &a,
                         int block, int variant, cudaStream_t s);
 
-/* The batch step kernel (one BatchArgs argument) of a storage form, for a
- * graph kernel node; *cta_threads receives its CTA size (pool blocks of
- * 256 nodes, 256 / CTA size CTAs each). */
+/* The batch step kernel (one BatchArgs argument) of a storage form with
+ * CTAs of `cta` threads (128 or 256; pool blocks of 256 nodes, 256 / cta
+ * CTAs each), for a graph kernel node; NULL for another size. */
 constexpr int kBatchBlock = 256;
-const void *batch_step_kernel(int precision, bool macros, int *cta_threads);
+const void *batch_step_kernel(int precision, bool macros, int cta);
 
 /* Fill the coefficients from tau, F and the storage scale. */
 void make_coeffs(double tau, double force, float scale, Coeffs *c);

@@ -628,57 +628,65 @@ int step_wave_blocks(int precision, int block, int variant)
     }
 }
 
-/* threads per CTA of the batch step: 128 for the fixed-point FP64 form
- * (two CTAs per pool block; 4% faster in the plain kernel), 256 otherwise */
-template <int PREC> struct BatchCta { static constexpr int v = PREC == PLB_FP64 ? 128 : kBatchBlock; };
-
-int batch_ctas_per_block(int precision)
+/* Threads per CTA of the batch step by default: 128 for the fixed-point
+ * FP64 form (two CTAs per pool block; 4% faster in the plain kernel), 256
+ * otherwise.  A pool may choose either (the launch tuner times both). */
+int batch_default_cta(int precision)
 {
-    return precision == PLB_FP64 ? kBatchBlock / BatchCta<PLB_FP64>::v : 1;
+    return precision == PLB_FP64 ? 128 : kBatchBlock;
 }
 
-template <int PREC>
-static int batch_wave_prec()
+template <int PREC, int BT>
+static int batch_wave_bt()
 {
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<PREC, false, BatchCta<PREC>::v>,
-                                                      BatchCta<PREC>::v, 0) != cudaSuccess)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<PREC, false, BT>, BT,
+                                                      0) != cudaSuccess)
         return 0;
     return sms * per;
 }
 
-int batch_wave_blocks(int precision)
+template <int PREC>
+static int batch_wave_prec(int cta)
+{
+    return cta == 128 ? batch_wave_bt<PREC, 128>() : batch_wave_bt<PREC, kBatchBlock>();
+}
+
+int batch_wave_blocks(int precision, int cta)
 {
     switch (precision) {
-    case PLB_FP64_EXACT: return batch_wave_prec<PLB_FP64_EXACT>();
-    case PLB_FP64: return batch_wave_prec<PLB_FP64>();
-    case PLB_FP64_FMA: return batch_wave_prec<PLB_FP64_FMA>();
-    case PLB_FP32: return batch_wave_prec<PLB_FP32>();
-    case PLB_FP16DEV: return batch_wave_prec<PLB_FP16DEV>();
-    case PLB_BF16DEV: return batch_wave_prec<PLB_BF16DEV>();
+    case PLB_FP64_EXACT: return batch_wave_prec<PLB_FP64_EXACT>(cta);
+    case PLB_FP64: return batch_wave_prec<PLB_FP64>(cta);
+    case PLB_FP64_FMA: return batch_wave_prec<PLB_FP64_FMA>(cta);
+    case PLB_FP32: return batch_wave_prec<PLB_FP32>(cta);
+    case PLB_FP16DEV: return batch_wave_prec<PLB_FP16DEV>(cta);
+    case PLB_BF16DEV: return batch_wave_prec<PLB_BF16DEV>(cta);
     default: return 0;
     }
 }
 
 template <int PREC>
-static const void *batch_fn(bool macros)
+static const void *batch_fn(bool macros, int cta)
 {
-    constexpr int BT = BatchCta<PREC>::v;
-    return macros ? (const void *)k_batch_step<PREC, true, BT>
-                  : (const void *)k_batch_step<PREC, false, BT>;
+    if (cta == 128)
+        return macros ? (const void *)k_batch_step<PREC, true, 128>
+                      : (const void *)k_batch_step<PREC, false, 128>;
+    return macros ? (const void *)k_batch_step<PREC, true, kBatchBlock>
+                  : (const void *)k_batch_step<PREC, false, kBatchBlock>;
 }
 
-const void *batch_step_kernel(int precision, bool macros, int *cta_threads)
+const void *batch_step_kernel(int precision, bool macros, int cta)
 {
+    if (cta != 128 && cta != kBatchBlock) return nullptr;
     switch (precision) {
-    case PLB_FP64_EXACT: *cta_threads = BatchCta<PLB_FP64_EXACT>::v; return batch_fn<PLB_FP64_EXACT>(macros);
-    case PLB_FP64: *cta_threads = BatchCta<PLB_FP64>::v; return batch_fn<PLB_FP64>(macros);
-    case PLB_FP64_FMA: *cta_threads = BatchCta<PLB_FP64_FMA>::v; return batch_fn<PLB_FP64_FMA>(macros);
-    case PLB_FP32: *cta_threads = BatchCta<PLB_FP32>::v; return batch_fn<PLB_FP32>(macros);
-    case PLB_FP16DEV: *cta_threads = BatchCta<PLB_FP16DEV>::v; return batch_fn<PLB_FP16DEV>(macros);
-    case PLB_BF16DEV: *cta_threads = BatchCta<PLB_BF16DEV>::v; return batch_fn<PLB_BF16DEV>(macros);
+    case PLB_FP64_EXACT: return batch_fn<PLB_FP64_EXACT>(macros, cta);
+    case PLB_FP64: return batch_fn<PLB_FP64>(macros, cta);
+    case PLB_FP64_FMA: return batch_fn<PLB_FP64_FMA>(macros, cta);
+    case PLB_FP32: return batch_fn<PLB_FP32>(macros, cta);
+    case PLB_FP16DEV: return batch_fn<PLB_FP16DEV>(macros, cta);
+    case PLB_BF16DEV: return batch_fn<PLB_BF16DEV>(macros, cta);
     default: return nullptr;
     }
 }

@@ -45,17 +45,25 @@ def _blocks_nodes(n):
 class Server:
     def __init__(self, hbm_budget_bytes, precision="fp32", check_every=250,
                  max_samples=4096, device=0, lookahead=64, batch=None,
-                 handoff_tol=None, handoff_share=0.35):
+                 handoff_tol=None, handoff_share=0.35, tuned=True):
         """precision: the storage form requests start in.  handoff_tol (only
         with "fp16dev"; default 1e-5): move a request to an FP32 pool once
         its relative change is below it; handoff_share: the FP32 pool's
-        share of the budget.  batch: a ready pool (tests)."""
+        share of the budget.  tuned: time the pool launch candidates of
+        the forms first (tune.ensure_pool, about a second per form, once per
+        process) and build the pools with the fastest.  batch: a ready pool
+        (tests)."""
         self.precision = precision
         self.lookahead = lookahead
         if precision == "fp16dev" and handoff_tol is None:
             handoff_tol = 1e-5
         self.handoff_tol = handoff_tol if precision == "fp16dev" else None
         self.tail = None
+        if batch is None and tuned:
+            from . import tune
+            tune.ensure_pool(precision, device)
+            if self.handoff_tol:
+                tune.ensure_pool("fp32", device)
         if batch is None:
             share = handoff_share if self.handoff_tol else 0.0
             cap = int(hbm_budget_bytes * (1 - share) // Batch.bytes_per_node(precision))
@@ -65,6 +73,7 @@ class Server:
                 self.tail = Batch(cap32, max_samples, "fp32", check_every, device=device)
         self.batch = batch
         self.capacity = int(batch.info()["capacity_nodes"])
+        self.pool_launch = getattr(batch, "launch_choice", None)
 
     @staticmethod
     def estimated_nodes(r):
@@ -206,6 +215,7 @@ class Server:
                        gpu_busy_s=busy_ms / 1e3,
                        gpu_idle_frac=max(0.0, 1.0 - busy_ms / 1e3 / wall) if wall > 0 else None,
                        handoffs=handoffs, handoff_tol=self.handoff_tol,
+                       pool_launch=self.pool_launch,
                        precision=self.precision, check_every=K,
                        rejected=[d["index"] for d in rejected])
         return done, summary

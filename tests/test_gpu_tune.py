@@ -32,3 +32,28 @@ def test_tune_picks_a_candidate_and_changes_no_result(precision):
         sim.close()
     # the node order may differ; the macros come back in reference order
     assert all((a == b).all() for a, b in zip(out[0], out[1]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pool_tuner_picks_a_candidate_caches_it_and_changes_no_result(precision):
+    """The pool tuner times batch-step CTAs of 128 and 256 threads with the
+    L2 prefetch on and off, caches the fastest for the form, and a pool
+    built afterwards takes it; every candidate gives the same bits."""
+    from porelb_gb300.batch import Batch
+    best, table = tune.tune_pool(precision, samples=4, edge=40, K=10)
+    assert len(table) == 4 and all(ms > 0 for *_, ms in table)
+    assert best["ms"] == min(ms for *_, ms in table)
+    assert tune.best_pool(precision) == {"cta_threads": best["cta_threads"],
+                                         "l2_prefetch": best["l2_prefetch"]}
+    with Batch(100000, 4, precision, check_every=10) as b:
+        assert b.launch_choice == tune.best_pool(precision)
+    dims = (24, 20, 16)
+    flag = pack_flag(dims, 5, 2.0, 4.0, 0.4)
+    ks = []
+    for cta, pf in [(c, p) for c in tune.POOL_CTAS for p in tune.POOL_PREFETCH]:
+        with Batch(50000, 2, precision, check_every=10, cta_threads=cta,
+                   l2_prefetch=pf) as b:
+            sid = b.add_flag(flag, *dims, 0.8, 1e-4, tol=0.0)
+            b.run(3)
+            ks.append((b.result(sid)["k_darcy"], b.get_f(sid)))
+    assert all(k == ks[0][0] and (f == ks[0][1]).all() for k, f in ks)
