@@ -366,6 +366,18 @@ void *plb_batch_stream(plb_batch *b);
 int plb_reduce_noalloc(const double *ux, const double *rho, long long n,
                        double *out, void *stream);
 
+/* ------------------------------------------------------ fault injection */
+
+/* Test hooks, no reference counterpart (the reference exits on a failed
+ * allocation, porelb.c:18-22,65-69).  Every device allocation the library
+ * makes is counted; after plb_fault_inject_alloc(n) with n > 0 the n-th
+ * allocation from then on fails once with PLB_ERR_NOMEM semantics (no
+ * cudaMalloc is called, so the GPU is not touched); n <= 0 disarms it.
+ * plb_alloc_count returns the allocations made so far, so that a test can
+ * count a call's allocations and fail each one in turn. */
+int plb_fault_inject_alloc(long long nth);
+long long plb_alloc_count(void);
+
 /* Human-readable text for a status code. */
 const char *plb_status_string(int status);
 

@@ -128,6 +128,8 @@ _SIGS = {
                                   ctypes.POINTER(ctypes.c_longlong)]),
     "plb_batch_stream": (_P, [_P]),
     "plb_reduce_noalloc": (_I, [_P, _P, ctypes.c_longlong, _P, _P]),
+    "plb_fault_inject_alloc": (_I, [ctypes.c_longlong]),
+    "plb_alloc_count": (ctypes.c_longlong, []),
 }
 
 _lib = None

@@ -392,7 +392,7 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     auto al = [&](auto **p, size_t bytes) {
-        if (e == cudaSuccess) e = cudaMalloc((void **)p, bytes ? bytes : 16);
+        if (e == cudaSuccess) e = plb_cuda_malloc((void **)p, bytes ? bytes : 16);
         b->bytes += bytes;
     };
     const size_t np = (size_t)b->npad;
@@ -486,8 +486,8 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     uint32_t *lexbits = nullptr, *lexoffs = nullptr;
     int n = 0, slab0 = 0, rc = PLB_OK;
     long long blk0 = -1, nblk = 0;
-    if (cudaMalloc(&lexbits, words * 4) != cudaSuccess ||
-        cudaMalloc(&lexoffs, words * 4) != cudaSuccess)
+    if (plb_cuda_malloc(&lexbits, words * 4) != cudaSuccess ||
+        plb_cuda_malloc(&lexoffs, words * 4) != cudaSuccess)
         rc = PLB_ERR_NOMEM;
     if (rc == PLB_OK) rc = flag_rank(dflag, nx, ny, nz, 1, lexbits, lexoffs, &n, &slab0, b->adm);
     if (rc == PLB_OK) {
@@ -560,7 +560,7 @@ int plb_batch_add_flag(plb_batch *b, const uint8_t *flag, int nx, int ny, int nz
     BCK(cudaSetDevice(b->device));
     const size_t cells = (size_t)nx * ny * nz;
     uint8_t *d = nullptr;
-    BCK(cudaMalloc(&d, cells));
+    BCK(plb_cuda_malloc(&d, cells));
     int rc = PLB_OK;
     if (cudaMemcpyAsync(d, flag, cells, cudaMemcpyHostToDevice, b->adm) != cudaSuccess)
         rc = PLB_ERR_CUDA;
@@ -582,7 +582,7 @@ int plb_batch_add_packed(plb_batch *b, uint64_t seed, int nx, int ny, int nz,
     BCK(cudaSetDevice(b->device));
     const size_t cells = (size_t)nx * ny * nz;
     uint8_t *d = nullptr;
-    BCK(cudaMalloc(&d, cells));
+    BCK(plb_cuda_malloc(&d, cells));
     int rc = sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, d, num_spheres,
                                 porosity_out, b->adm);
     if (rc == PLB_OK) rc = add_dflag(b, d, nx, ny, nz, sp, id);
@@ -1041,7 +1041,7 @@ int plb_batch_get_f(plb_batch *b, int id, double *f_aos)
     if (h.n == 0) return PLB_OK;
     double *d = nullptr;
     const size_t bytes = 8 * Q * (size_t)h.n;
-    BCK(cudaMalloc(&d, bytes));
+    BCK(plb_cuda_malloc(&d, bytes));
     const long long base = h.blk0 * B;
     const float inv = 1.0f / h.scale;
     const void *f = b->f[b->cur];
@@ -1071,7 +1071,7 @@ int plb_batch_get_macros(plb_batch *b, int id, double *rho, double *ux,
     const SampleHost &h = b->s[id];
     if (h.n == 0) return PLB_OK;
     double *d = nullptr;
-    BCK(cudaMalloc(&d, 8 * 4 * (size_t)h.n));
+    BCK(plb_cuda_malloc(&d, 8 * 4 * (size_t)h.n));
     k_get_macro_sample<<<gb(h.n, B), B, 0, b->st>>>(b->macro, b->npad, h.blk0 * B, h.n,
                                                    b->perm, d);
     double *dst[4] = {rho, ux, uy, uz};

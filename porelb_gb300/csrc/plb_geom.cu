@@ -285,10 +285,10 @@ int sphere_pack_device(uint64_t seed, int nx, int ny, int nz, double rmin,
     const double v = 4.18879020478639 * rm * rm * rm;
     long long chunk = (long long)(-log(porosity > 1e-6 ? porosity : 1e-6) * total / v * 1.3) + 64;
     if (chunk > 4000000) chunk = 4000000;
-    CKG(cudaMalloc(&first, cells * 4));
+    CKG(plb_cuda_malloc(&first, cells * 4));
     CKG(cudaMemsetAsync(first, 0xff, cells * 4, st));
-    CKG(cudaMalloc(&dsp, sizeof(Sphere) * (size_t)chunk));
-    CKG(cudaMalloc(&hist, sizeof(unsigned long long) * (size_t)chunk));
+    CKG(plb_cuda_malloc(&dsp, sizeof(Sphere) * (size_t)chunk));
+    CKG(plb_cuda_malloc(&hist, sizeof(unsigned long long) * (size_t)chunk));
     hsp = (Sphere *)malloc(sizeof(Sphere) * (size_t)chunk);
     hh = (unsigned long long *)malloc(sizeof(unsigned long long) * (size_t)chunk);
     if (!hsp || !hh) { rc = PLB_ERR_NOMEM; goto done; }
@@ -346,8 +346,8 @@ int flag_rank(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
     unsigned *bad = nullptr;
     uint32_t *cnt = nullptr;
     unsigned hbad = 0;
-    CKG(cudaMalloc(&bad, 4));
-    CKG(cudaMalloc(&cnt, words * 4));
+    CKG(plb_cuda_malloc(&bad, 4));
+    CKG(plb_cuda_malloc(&cnt, words * 4));
     CKG(cudaMemsetAsync(bad, 0, 4, st));
     k_flag_bits<<<gsz(words, 256), 256, 0, st>>>(dflag, cells, lexbits, cnt, words, bad);
     CKG(cudaGetLastError());
@@ -402,9 +402,9 @@ int flag_tables(const uint8_t *dflag, int nx, int ny, int nz, int num_p,
     int rc = PLB_OK;
     uint32_t *obits = nullptr, *ooffs = nullptr, *ocnt = nullptr;
     if (n == 0) return PLB_OK;
-    CKG(cudaMalloc(&obits, owords * 4));
-    CKG(cudaMalloc(&ooffs, owords * 4));
-    CKG(cudaMalloc(&ocnt, owords * 4));
+    CKG(plb_cuda_malloc(&obits, owords * 4));
+    CKG(plb_cuda_malloc(&ooffs, owords * 4));
+    CKG(plb_cuda_malloc(&ocnt, owords * 4));
     CKG(cudaMemsetAsync(obits, 0, owords * 4, st));
     k_mark_order<<<gsz(cells, 256), 256, 0, st>>>(lexbits, g, cells, obits);
     CKG(cudaGetLastError());

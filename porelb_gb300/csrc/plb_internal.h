@@ -10,6 +10,16 @@
 #include "porelb_gpu.h"
 #include "plb_fx.h"
 
+/* Every device allocation of the library goes through here, so that a test
+ * can make one of them fail on the host (plb_fault_inject_alloc) and drive
+ * the out-of-memory paths without touching the GPU. */
+cudaError_t plb_dev_malloc(void **p, size_t bytes);
+template <typename P>
+static inline cudaError_t plb_cuda_malloc(P **p, size_t bytes)
+{
+    return plb_dev_malloc((void **)p, bytes);
+}
+
 namespace plb {
 
 constexpr int Q = 19;

@@ -15,6 +15,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "plb_internal.h"
 
 using namespace plb;
@@ -58,9 +60,38 @@ struct plb_sim {
         if (e_ != cudaSuccess) {                                          \
             fprintf(stderr, "porelb_gpu: %s failed: %s (%s:%d)\n", #call, \
                     cudaGetErrorString(e_), __FILE__, __LINE__);          \
-            return PLB_ERR_CUDA;                                          \
+            return e_ == cudaErrorMemoryAllocation ? PLB_ERR_NOMEM        \
+                                                   : PLB_ERR_CUDA;        \
         }                                                                 \
     } while (0)
+
+/* ------------------------------------------------------ allocation */
+
+/* Device allocations made so far and the armed failure (0 = none): the
+ * fault_at-th allocation after plb_fault_inject_alloc reports
+ * cudaErrorMemoryAllocation without calling cudaMalloc. */
+static std::atomic<long long> g_allocs{0};
+static std::atomic<long long> g_fault_at{0};
+
+cudaError_t plb_dev_malloc(void **p, size_t bytes)
+{
+    const long long k = ++g_allocs;
+    const long long at = g_fault_at.load();
+    if (at > 0 && k == at) {
+        g_fault_at.store(0);
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes ? bytes : 16);
+}
+
+int plb_fault_inject_alloc(long long nth)
+{
+    g_fault_at.store(nth > 0 ? g_allocs.load() + nth : 0);
+    return PLB_OK;
+}
+
+long long plb_alloc_count(void) { return g_allocs.load(); }
 
 /* ---------------------------------------------------------------- scan */
 
@@ -186,7 +217,7 @@ int scan_words(const uint32_t *cnt, uint32_t *offs, size_t m, cudaStream_t st)
 {
     const size_t ntiles = (m + kScanTile - 1) / kScanTile;
     uint32_t *tmp = nullptr;
-    if (cudaMalloc(&tmp, ntiles * 4 + 4) != cudaSuccess) return PLB_ERR_NOMEM;
+    if (plb_cuda_malloc(&tmp, ntiles * 4 + 4) != cudaSuccess) return PLB_ERR_NOMEM;
     int rc = exclusive_scan(cnt, offs, m, tmp, st);
     cudaStreamSynchronize(st);
     cudaFree(tmp);
@@ -545,7 +576,7 @@ template <typename P>
 static cudaError_t dev_alloc(P **p, size_t bytes, size_t *acc)
 {
     *acc += bytes;
-    return cudaMalloc((void **)p, bytes ? bytes : 16);
+    return plb_cuda_malloc((void **)p, bytes ? bytes : 16);
 }
 
 static int build_tables(plb_sim *s, const plb_node_info *V_host)
@@ -764,8 +795,8 @@ static int create_from_dflag(const uint8_t *dflag, int nx, int ny, int nz,
     int rc = PLB_OK, n = 0;
     plb_sim *s = nullptr;
     if (!slab) return PLB_ERR_NOMEM;
-    if (cudaMalloc(&lexbits, words * 4) != cudaSuccess ||
-        cudaMalloc(&lexoffs, words * 4) != cudaSuccess) {
+    if (plb_cuda_malloc(&lexbits, words * 4) != cudaSuccess ||
+        plb_cuda_malloc(&lexoffs, words * 4) != cudaSuccess) {
         rc = PLB_ERR_NOMEM;
     }
     if (rc == PLB_OK)
@@ -808,7 +839,7 @@ int plb_create_from_flag(const uint8_t *flag, int nx, int ny, int nz,
     cudaStream_t st;
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     int rc = PLB_OK;
-    if (cudaMalloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
+    if (plb_cuda_malloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
     if (rc == PLB_OK && cudaMemcpyAsync(dflag, flag, cells, cudaMemcpyHostToDevice, st) != cudaSuccess)
         rc = PLB_ERR_CUDA;
     if (rc == PLB_OK) rc = create_from_dflag(dflag, nx, ny, nz, num_p, p, st, out);
@@ -831,7 +862,7 @@ int plb_sphere_pack_device(uint64_t seed, int nx, int ny, int nz, double rmin,
     cudaStream_t st;
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     int rc = PLB_OK;
-    if (cudaMalloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
+    if (plb_cuda_malloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
     if (rc == PLB_OK)
         rc = sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, dflag,
                                 num_spheres, porosity_out, st);
@@ -867,7 +898,7 @@ int plb_create_packed(uint64_t seed, int nx, int ny, int nz, double rmin,
     cudaStream_t st;
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     int rc = PLB_OK;
-    if (cudaMalloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
+    if (plb_cuda_malloc(&dflag, cells) != cudaSuccess) rc = PLB_ERR_NOMEM;
     if (rc == PLB_OK)
         rc = sphere_pack_device(seed, nx, ny, nz, rmin, rmax, porosity, dflag,
                                 num_spheres, porosity_out, st);
@@ -987,7 +1018,7 @@ int plb_get_macros(plb_sim *s, double *rho, double *ux, double *uy, double *uz)
     if (s->n == 0) return PLB_OK;
     CK(cudaSetDevice(s->device));
     double *d = nullptr;
-    CK(cudaMalloc(&d, sizeof(double) * 4 * (size_t)s->n));
+    CK(plb_cuda_malloc(&d, sizeof(double) * 4 * (size_t)s->n));
     k_get_macro<<<nblk(s->n, 256), 256, 0, s->stream>>>(s->macro, s->perm, s->npad, s->n, d);
     double *dst[4] = {rho, ux, uy, uz};
     cudaError_t e = cudaGetLastError();
@@ -1034,7 +1065,7 @@ int plb_get_f(plb_sim *s, double *f_aos)
     CK(cudaSetDevice(s->device));
     double *d = nullptr;
     const size_t bytes = sizeof(double) * Q * (size_t)s->n;
-    CK(cudaMalloc(&d, bytes));
+    CK(plb_cuda_malloc(&d, bytes));
     const unsigned g = nblk(s->n, 256);
     const void *f = s->f[s->cur];
     switch (s->precision) {
@@ -1064,7 +1095,7 @@ int plb_set_f(plb_sim *s, const double *f_aos)
     CK(cudaSetDevice(s->device));
     double *d = nullptr;
     const size_t bytes = sizeof(double) * Q * (size_t)s->n;
-    CK(cudaMalloc(&d, bytes));
+    CK(plb_cuda_malloc(&d, bytes));
     cudaError_t e = cudaMemcpyAsync(d, f_aos, bytes, cudaMemcpyHostToDevice, s->stream);
     const unsigned g = nblk(s->n, 256);
     void *f = s->f[s->cur];
@@ -1096,7 +1127,7 @@ int plb_get_f_streamed(plb_sim *s, double *f_aos)
     CK(cudaSetDevice(s->device));
     double *d = nullptr;
     const size_t bytes = sizeof(double) * Q * (size_t)s->n;
-    CK(cudaMalloc(&d, bytes));
+    CK(plb_cuda_malloc(&d, bytes));
     const unsigned g = nblk(s->n, 256);
     const void *f = s->f[s->cur];
     const float inv = 1.0f / s->scale;
