@@ -289,7 +289,10 @@ typedef struct {
     int l2_prefetch;       /* L2 prefetch of the pool block half a wave
                               ahead: 0 = default (on for PLB_FP64), 1 on,
                               -1 off */
-    int reserved[6];
+    int ordering;          /* node order within each sample:
+                              PLB_ORDER_MORTON (0, default) or
+                              PLB_ORDER_REFERENCE */
+    int reserved[5];
 } plb_batch_params;
 int plb_batch_create_ex(const plb_batch_params *p, plb_batch **out);
 void plb_batch_destroy(plb_batch *b);

@@ -11,7 +11,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .api import PRECISIONS, PorelbError, _check, _ptr
+from .api import ORDERINGS, PRECISIONS, PorelbError, _check, _ptr
 
 STATUS = {0: "running", 1: "converged", 2: "step limit", 3: "released",
           4: "parked"}
@@ -21,20 +21,23 @@ PARKED = 4
 class Batch:
     def __init__(self, capacity_nodes, max_samples=1024, precision="fp32",
                  check_every=1000, keep_macros=False, device=0, cta_threads=None,
-                 l2_prefetch=None):
-        """cta_threads (128 or 256) and l2_prefetch (True/False): the batch
-        step's launch; None takes the launch tuner's cached choice for this
+                 l2_prefetch=None, ordering=None):
+        """cta_threads (128 or 256), l2_prefetch (True/False) and ordering
+        ("morton" or "reference"): the batch step's launch and the samples'
+        node order; None takes the launch tuner's cached choice for this
         form (porelb_gb300.tune.tune_pool), else the library default."""
         self._lib = _lib.load()
         self.precision = precision
         self.check_every = check_every
-        if cta_threads is None or l2_prefetch is None:
+        if cta_threads is None or l2_prefetch is None or ordering is None:
             from . import tune
             choice = tune.best_pool(precision)
             if cta_threads is None:
                 cta_threads = choice["cta_threads"]
             if l2_prefetch is None:
                 l2_prefetch = choice["l2_prefetch"]
+            if ordering is None:
+                ordering = choice["ordering"]
         bp = _lib.BatchParams()
         bp.capacity_nodes = int(capacity_nodes)
         bp.max_samples = max_samples
@@ -44,11 +47,13 @@ class Batch:
         bp.device = device
         bp.cta_threads = int(cta_threads or 0)
         bp.l2_prefetch = 0 if l2_prefetch is None else (1 if l2_prefetch else -1)
+        bp.ordering = ORDERINGS[ordering or "morton"]
         h = ctypes.c_void_p()
         _check(self._lib.plb_batch_create_ex(ctypes.byref(bp), ctypes.byref(h)),
                "plb_batch_create_ex")
         self._h = h
-        self.launch_choice = dict(cta_threads=cta_threads, l2_prefetch=l2_prefetch)
+        self.launch_choice = dict(cta_threads=cta_threads, l2_prefetch=l2_prefetch,
+                                  ordering=ordering)
         self.meta = {}
 
     @staticmethod

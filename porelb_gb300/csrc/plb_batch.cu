@@ -251,6 +251,7 @@ struct plb_batch {
     float last_ms = 0.f;
     bool in_flight = false;
     int cta = 256;     /* threads per CTA of the batch step */
+    int ordering = PLB_ORDER_MORTON; /* node order of each sample's table */
     int prefetch = 0;  /* L2 prefetch of the pool block half a wave ahead */
     long long cap_blocks = 0, npad = 0, rest = 0;
     void *f[2] = {nullptr, nullptr};
@@ -363,7 +364,8 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     const int check_every = bp->check_every, keep_macros = bp->keep_macros;
     const int device = bp->device;
     if ((bp->cta_threads != 0 && bp->cta_threads != 128 && bp->cta_threads != B) ||
-        bp->l2_prefetch < -1 || bp->l2_prefetch > 1)
+        bp->l2_prefetch < -1 || bp->l2_prefetch > 1 ||
+        (bp->ordering != PLB_ORDER_MORTON && bp->ordering != PLB_ORDER_REFERENCE))
         return PLB_ERR_ARG;
     if (capacity_nodes == 0 || max_samples <= 0 || max_samples > (1 << 22) ||
         elem_of(precision) == 0 ||
@@ -381,6 +383,7 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     b->max_samples = max_samples;
     b->elem = elem_of(precision);
     b->cta = bp->cta_threads ? bp->cta_threads : batch_default_cta(precision);
+    b->ordering = bp->ordering;
     b->prefetch = bp->l2_prefetch > 0 || (bp->l2_prefetch == 0 && precision == PLB_FP64);
     b->cap_blocks = (long long)((capacity_nodes + B - 1) / B);
     b->rest = b->cap_blocks * B;
@@ -498,7 +501,7 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     }
     if (rc == PLB_OK) {
         const long long base = blk0 * B;
-        rc = flag_tables(dflag, nx, ny, nz, 1, PLB_ORDER_MORTON, 0, 0, lexbits, lexoffs, n,
+        rc = flag_tables(dflag, nx, ny, nz, 1, b->ordering, 0, 0, lexbits, lexoffs, n,
                          b->npad, b->perm + base, b->coord + base, b->nbr + base,
                          (uint32_t)base, (uint32_t)b->rest, b->adm);
         if (rc != PLB_OK) free_range(b, blk0, nblk);

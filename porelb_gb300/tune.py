@@ -10,8 +10,9 @@ ordering and L2 prefetch.
   uses.
 * ``tune_pool`` (batched pool and server): for one storage form it builds a
   pool of synthetic sphere packs per candidate (batch-step CTAs of 128 or
-  256 threads, L2 prefetch of the pool block half a wave ahead on or off),
-  times intervals of the batch step, and keeps the fastest.  Cached per
+  256 threads, L2 prefetch of the pool block half a wave ahead on or off,
+  Morton or reference node order within each sample), times intervals of
+  the batch step, and keeps the fastest.  Cached per
   form; every ``Batch`` created without an explicit launch takes the cached
   choice (``best_pool``), and ``Server`` tunes its pools' form when it
   starts.
@@ -28,6 +29,7 @@ BLOCKS = (64, 128, 256)
 ORDERINGS = ("morton", "reference")
 POOL_CTAS = (128, 256)
 POOL_PREFETCH = (False, True)
+POOL_ORDERINGS = ("morton", "reference")
 _cache = {}
 _pool_cache = {}
 
@@ -83,13 +85,13 @@ def best(precision, n, boundary="reference"):
 
 
 def time_pool(precision, cta_threads, l2_prefetch, samples=8, edge=64, K=20,
-              intervals=3, device=0):
+              intervals=3, device=0, ordering="morton"):
     """Milliseconds per lattice step of a pool of `samples` sphere packs of
     edge^3 (seeds 200+, R ~ U[3, 6], porosity 0.35) with this launch."""
     from .batch import Batch
     cap = int(samples * (edge ** 3 * 0.40 + 512))
     with Batch(cap, samples, precision, check_every=K, device=device,
-               cta_threads=cta_threads, l2_prefetch=l2_prefetch) as b:
+               cta_threads=cta_threads, l2_prefetch=l2_prefetch, ordering=ordering) as b:
         for k in range(samples):
             b.add_packed(200 + k, edge, edge, edge, 3.0, 6.0, 0.35, 0.8, 5e-7,
                          tol=0.0, max_steps=10 ** 9)
@@ -104,21 +106,23 @@ def time_pool(precision, cta_threads, l2_prefetch, samples=8, edge=64, K=20,
 
 def tune_pool(precision, samples=8, edge=64, K=20, device=0):
     """Time every pool launch candidate for this form; caches and returns
-    (best, [(cta_threads, l2_prefetch, ms per step)])."""
+    (best, [(cta_threads, l2_prefetch, ordering, ms per step)])."""
     table = []
-    for cta in POOL_CTAS:
-        for pf in POOL_PREFETCH:
-            table.append((cta, pf, time_pool(precision, cta, pf, samples, edge, K,
-                                             device=device)))
-    best = min(table, key=lambda r: r[2])
-    choice = dict(cta_threads=best[0], l2_prefetch=best[1])
+    for order in POOL_ORDERINGS:
+        for cta in POOL_CTAS:
+            for pf in POOL_PREFETCH:
+                table.append((cta, pf, order, time_pool(precision, cta, pf, samples, edge, K,
+                                                        device=device, ordering=order)))
+    best = min(table, key=lambda r: r[3])
+    choice = dict(cta_threads=best[0], l2_prefetch=best[1], ordering=best[2])
     _pool_cache[precision] = choice
-    return dict(choice, ms=best[2]), table
+    return dict(choice, ms=best[3]), table
 
 
 def best_pool(precision):
     """Cached pool launch for this form, or the library defaults (None)."""
-    return _pool_cache.get(precision, dict(cta_threads=None, l2_prefetch=None))
+    return _pool_cache.get(precision, dict(cta_threads=None, l2_prefetch=None,
+                                           ordering=None))
 
 
 def ensure_pool(precision, device=0):

@@ -41,18 +41,19 @@ def test_pool_tuner_picks_a_candidate_caches_it_and_changes_no_result(precision)
     built afterwards takes it; every candidate gives the same bits."""
     from porelb_gb300.batch import Batch
     best, table = tune.tune_pool(precision, samples=4, edge=40, K=10)
-    assert len(table) == 4 and all(ms > 0 for *_, ms in table)
+    assert len(table) == 8 and all(ms > 0 for *_, ms in table)
     assert best["ms"] == min(ms for *_, ms in table)
-    assert tune.best_pool(precision) == {"cta_threads": best["cta_threads"],
-                                         "l2_prefetch": best["l2_prefetch"]}
+    assert tune.best_pool(precision) == {k: best[k] for k in
+                                         ("cta_threads", "l2_prefetch", "ordering")}
     with Batch(100000, 4, precision, check_every=10) as b:
         assert b.launch_choice == tune.best_pool(precision)
     dims = (24, 20, 16)
     flag = pack_flag(dims, 5, 2.0, 4.0, 0.4)
     ks = []
-    for cta, pf in [(c, p) for c in tune.POOL_CTAS for p in tune.POOL_PREFETCH]:
+    for cta, pf, order in [(c, p, o) for c in tune.POOL_CTAS for p in tune.POOL_PREFETCH
+                           for o in tune.POOL_ORDERINGS]:
         with Batch(50000, 2, precision, check_every=10, cta_threads=cta,
-                   l2_prefetch=pf) as b:
+                   l2_prefetch=pf, ordering=order) as b:
             sid = b.add_flag(flag, *dims, 0.8, 1e-4, tol=0.0)
             b.run(3)
             ks.append((b.result(sid)["k_darcy"], b.get_f(sid)))
