@@ -412,7 +412,8 @@ def run_gpu(args, rank, world, local):
         "data": DATA,
         "config": workload_config(args.workload, w, N, phi, prec),
         "parallelism": f"replicas{world}",
-        "layout": "SoA f[19][npad] ping-pong, Morton node order",
+        "layout": "SoA f[19][npad] ping-pong, %s node order"
+                  % P.auto_ordering(N, dims[2], prec, local),
         "k_darcy_after_run": kd, "steady_state": steady,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s",

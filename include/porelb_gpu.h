@@ -73,8 +73,18 @@ enum {
     PLB_FP64_FMA = 5    /* FP64 storage, FMA-contracted FP64 collision */
 };
 
-/* Node ordering in device memory. */
-enum { PLB_ORDER_MORTON = 0, PLB_ORDER_REFERENCE = 1 };
+/* Node ordering in device memory (the same results in every order).
+ * REFERENCE is the table's own row order (x fastest, then y, then z): a
+ * warp's 32 consecutive nodes then have their neighbours in every direction
+ * in one shifted run of nodes, which gathers best while the three z-planes
+ * a step reads at once stay in L2.  MORTON keeps the gathers local at any
+ * size.  AUTO takes REFERENCE when three z-planes of the domain's nodes fit
+ * in half the L2, else MORTON (256^3: reference order, FP64 17.2 against
+ * 16.4 GLUPS; 512^3 FP64 and 1024^3: Morton). */
+enum { PLB_ORDER_MORTON = 0, PLB_ORDER_REFERENCE = 1, PLB_ORDER_AUTO = 2 };
+/* The order AUTO picks for n nodes in an nx*ny*nz domain with elem-byte
+ * storage on device `device`. */
+int plb_auto_ordering(long long n, int nz, int elem_bytes, int device);
 
 /* Wall rule. */
 enum {
@@ -99,7 +109,8 @@ typedef struct {
     double tau;      /* relaxation time; reference hard-codes 0.8 (porelb.c:87) */
     double force_x;  /* body force along x; reference hard-codes 1e-3 (porelb.c:91) */
     int precision;   /* PLB_FP64_EXACT ... */
-    int ordering;    /* PLB_ORDER_MORTON or PLB_ORDER_REFERENCE */
+    int ordering;    /* PLB_ORDER_AUTO (default), PLB_ORDER_MORTON or
+                        PLB_ORDER_REFERENCE */
     int halo;        /* PLB_HALO_* */
     int block_size;  /* threads per block for the step kernel; 0 = default */
     int device;      /* CUDA device ordinal */
@@ -290,8 +301,9 @@ typedef struct {
                               ahead: 0 = default (on for PLB_FP64), 1 on,
                               -1 off */
     int ordering;          /* node order within each sample:
-                              PLB_ORDER_MORTON (0, default) or
-                              PLB_ORDER_REFERENCE */
+                              PLB_ORDER_MORTON (0, default),
+                              PLB_ORDER_REFERENCE or PLB_ORDER_AUTO (chosen
+                              per sample) */
     int reserved[5];
 } plb_batch_params;
 int plb_batch_create_ex(const plb_batch_params *p, plb_batch **out);

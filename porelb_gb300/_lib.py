@@ -28,7 +28,7 @@ ERR_ARG, ERR_IO, ERR_TABLE, ERR_CUDA = -1, -2, -3, -4
 ERR_NOMEM, ERR_DENSITY, ERR_NUMP, ERR_STATE = -5, -6, -7, -8
 
 FP64_EXACT, FP64, FP32, FP16DEV, BF16DEV, FP64_FMA = 0, 1, 2, 3, 4, 5
-ORDER_MORTON, ORDER_REFERENCE = 0, 1
+ORDER_MORTON, ORDER_REFERENCE, ORDER_AUTO = 0, 1, 2
 HALO_AUTO, HALO_SINGLE, HALO_REMOTE_WINS = -1, 0, 1
 REDUCE_NOALLOC_MAX_NODES = 67108864
 BOUNDARY_REFERENCE, BOUNDARY_HALFWAY = 0, 1
@@ -129,6 +129,7 @@ _SIGS = {
     "plb_batch_stream": (_P, [_P]),
     "plb_reduce_noalloc": (_I, [_P, _P, ctypes.c_longlong, _P, _P]),
     "plb_fault_inject_alloc": (_I, [ctypes.c_longlong]),
+    "plb_auto_ordering": (_I, [ctypes.c_longlong, _I, _I, _I]),
     "plb_alloc_count": (ctypes.c_longlong, []),
 }
 

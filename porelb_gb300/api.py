@@ -20,7 +20,8 @@ from ._lib import NODE_DTYPE, Q
 PRECISIONS = {"fp64_exact": _lib.FP64_EXACT, "fp64": _lib.FP64,
               "fp32": _lib.FP32, "fp16dev": _lib.FP16DEV,
               "bf16dev": _lib.BF16DEV, "fp64_fma": _lib.FP64_FMA}
-ORDERINGS = {"morton": _lib.ORDER_MORTON, "reference": _lib.ORDER_REFERENCE}
+ORDERINGS = {"morton": _lib.ORDER_MORTON, "reference": _lib.ORDER_REFERENCE,
+             "auto": _lib.ORDER_AUTO}
 HALOS = {"auto": _lib.HALO_AUTO, "single": _lib.HALO_SINGLE,
          "remote_wins": _lib.HALO_REMOTE_WINS}
 BOUNDARIES = {"reference": _lib.BOUNDARY_REFERENCE,
@@ -140,6 +141,16 @@ def _params(tau, force, precision, ordering, halo, block_size, device,
     return p
 
 
+def auto_ordering(num_node, nz, precision, device=0):
+    """The node order PLB_ORDER_AUTO picks for this domain and form:
+    "reference" (row order) when three z-planes of its nodes fit in half the
+    L2, else "morton"."""
+    elem = {"fp64_exact": 8, "fp64": 8, "fp64_fma": 8, "fp32": 4, "fp16dev": 2,
+            "bf16dev": 2}[precision]
+    o = _lib.load().plb_auto_ordering(int(num_node), int(nz), elem, device)
+    return "reference" if o == _lib.ORDER_REFERENCE else "morton"
+
+
 def _tuned(precision, n, boundary):
     from . import tune
     c = tune.best(precision, n, boundary)
@@ -152,7 +163,7 @@ class Simulation:
     """One solver instance on one GPU (a SIMULATION of porelb.h:79-117)."""
 
     def __init__(self, V, nx, ny, nz, v_sub_start=None, tau=0.8,
-                 force=1e-3, precision="fp64_exact", ordering="morton",
+                 force=1e-3, precision="fp64_exact", ordering="auto",
                  halo="auto", block_size=0, device=0, boundary="reference",
                  kernel_variant=0, prefetch=None, tuned=False):
         """tuned: take block size, ordering and register budget from the
@@ -288,7 +299,7 @@ class Simulation:
 
     @classmethod
     def from_flag(cls, flag, nx, ny, nz, num_p=1, tau=0.8, force=1e-3,
-                  precision="fp64_exact", ordering="morton", halo="auto",
+                  precision="fp64_exact", ordering="auto", halo="auto",
                   block_size=0, device=0, boundary="reference",
                   kernel_variant=0, prefetch=None, tuned=False):
         """build_V + create on the device from a 0/1 flag grid."""
@@ -309,7 +320,7 @@ class Simulation:
 
     @classmethod
     def packed(cls, seed, nx, ny, nz, rmin, rmax, porosity, num_p=1, tau=0.8,
-               force=1e-3, precision="fp64", ordering="morton", halo="auto",
+               force=1e-3, precision="fp64", ordering="auto", halo="auto",
                block_size=0, device=0, boundary="reference", kernel_variant=0,
                prefetch=None):
         """Sphere pack, table and handle, all built on the device."""

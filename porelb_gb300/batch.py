@@ -47,7 +47,7 @@ class Batch:
         bp.device = device
         bp.cta_threads = int(cta_threads or 0)
         bp.l2_prefetch = 0 if l2_prefetch is None else (1 if l2_prefetch else -1)
-        bp.ordering = ORDERINGS[ordering or "morton"]
+        bp.ordering = ORDERINGS[ordering or "auto"]
         h = ctypes.c_void_p()
         _check(self._lib.plb_batch_create_ex(ctypes.byref(bp), ctypes.byref(h)),
                "plb_batch_create_ex")

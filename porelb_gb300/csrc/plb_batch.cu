@@ -365,7 +365,8 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     const int device = bp->device;
     if ((bp->cta_threads != 0 && bp->cta_threads != 128 && bp->cta_threads != B) ||
         bp->l2_prefetch < -1 || bp->l2_prefetch > 1 ||
-        (bp->ordering != PLB_ORDER_MORTON && bp->ordering != PLB_ORDER_REFERENCE))
+        (bp->ordering != PLB_ORDER_MORTON && bp->ordering != PLB_ORDER_REFERENCE &&
+         bp->ordering != PLB_ORDER_AUTO))
         return PLB_ERR_ARG;
     if (capacity_nodes == 0 || max_samples <= 0 || max_samples > (1 << 22) ||
         elem_of(precision) == 0 ||
@@ -501,7 +502,10 @@ static int add_dflag(plb_batch *b, const uint8_t *dflag, int nx, int ny, int nz,
     }
     if (rc == PLB_OK) {
         const long long base = blk0 * B;
-        rc = flag_tables(dflag, nx, ny, nz, 1, b->ordering, 0, 0, lexbits, lexoffs, n,
+        const int order = b->ordering == PLB_ORDER_AUTO
+                              ? plb_auto_ordering(n, nz, (int)b->elem, b->device)
+                              : b->ordering;
+        rc = flag_tables(dflag, nx, ny, nz, 1, order, 0, 0, lexbits, lexoffs, n,
                          b->npad, b->perm + base, b->coord + base, b->nbr + base,
                          (uint32_t)base, (uint32_t)b->rest, b->adm);
         if (rc != PLB_OK) free_range(b, blk0, nblk);

@@ -27,7 +27,7 @@ void plb_default_params(plb_params *p)
     p->tau = 0.8;       /* porelb.c:87 */
     p->force_x = 1e-3;  /* porelb.c:91 */
     p->precision = PLB_FP64_EXACT;
-    p->ordering = PLB_ORDER_MORTON;
+    p->ordering = PLB_ORDER_AUTO;
     p->halo = PLB_HALO_AUTO;
     p->block_size = 0;
     p->device = 0;

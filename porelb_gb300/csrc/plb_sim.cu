@@ -65,6 +65,20 @@ struct plb_sim {
         }                                                                 \
     } while (0)
 
+/* ------------------------------------------------------ ordering */
+
+int plb_auto_ordering(long long n, int nz, int elem_bytes, int device)
+{
+    /* bytes a step moves per node: 19 values in and out, 18 words, perm */
+    const double bpn = 2.0 * 19 * elem_bytes + 72 + 4;
+    int l2 = 0;
+    if (nz <= 0 || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device) != cudaSuccess ||
+        l2 <= 0)
+        return PLB_ORDER_MORTON;
+    const double plane = bpn * (double)n / nz;
+    return 3.0 * plane <= 0.5 * (double)l2 ? PLB_ORDER_REFERENCE : PLB_ORDER_MORTON;
+}
+
 /* ------------------------------------------------------ allocation */
 
 /* Device allocations made so far and the armed failure (0 = none): the
@@ -673,7 +687,8 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     *out = nullptr;
     if (n < 0 || nx <= 0 || ny <= 0 || nz <= 0 || num_p <= 0 || !v_sub_start ||
         !(p->tau > 0.5) || !isfinite(p->force_x) || elem_size(p->precision) == 0 ||
-        (p->ordering != PLB_ORDER_MORTON && p->ordering != PLB_ORDER_REFERENCE) ||
+        (p->ordering != PLB_ORDER_MORTON && p->ordering != PLB_ORDER_REFERENCE &&
+         p->ordering != PLB_ORDER_AUTO) ||
         (p->boundary != PLB_BOUNDARY_REFERENCE && p->boundary != PLB_BOUNDARY_HALFWAY) ||
         n >= kMaxNodes)
         return PLB_ERR_ARG;
@@ -696,7 +711,9 @@ static int sim_alloc(const plb_params *p, int n, int nx, int ny, int nz,
     s->num_p = num_p;
     s->npad = ((long long)n + 1 + 63) / 64 * 64;
     s->precision = p->precision;
-    s->ordering = p->ordering;
+    s->ordering = p->ordering == PLB_ORDER_AUTO
+                      ? plb_auto_ordering(n, nz, (int)elem_size(p->precision), p->device)
+                      : p->ordering;
     s->halo = p->halo;
     s->boundary = p->boundary;
     /* register budget of the step kernel (kernel_variant 1 and 3 are the

@@ -81,7 +81,7 @@ def tune(flag, dims, precision="fp64", boundary="reference", steps=20):
 def best(precision, n, boundary="reference"):
     """Cached choice for this form and size, or the defaults."""
     return _cache.get((precision, boundary, _bucket(n)),
-                      dict(block_size=0, ordering="morton", kernel_variant=0))
+                      dict(block_size=0, ordering="auto", kernel_variant=0))
 
 
 def time_pool(precision, cta_threads, l2_prefetch, samples=8, edge=64, K=20,

@@ -58,3 +58,25 @@ def test_pool_tuner_picks_a_candidate_caches_it_and_changes_no_result(precision)
             b.run(3)
             ks.append((b.result(sid)["k_darcy"], b.get_f(sid)))
     assert all(k == ks[0][0] and (f == ks[0][1]).all() for k, f in ks)
+
+
+def test_auto_ordering_picks_row_order_while_three_planes_fit_in_l2():
+    """PLB_ORDER_AUTO: row (reference) order for the 256^3 FP64 workload and
+    the 512^3 16-bit form, Morton for 512^3 FP64 and the 1024^3 forms
+    (measured fastest on GB300 in each case); both orders give the same
+    bits."""
+    assert P.auto_ordering(5871717, 256, "fp64") == "reference"
+    assert P.auto_ordering(91750000, 512, "fp16dev") == "reference"
+    assert P.auto_ordering(91750000, 512, "fp64") == "morton"
+    assert P.auto_ordering(214748328, 1024, "fp16dev") == "morton"
+    dims = (40, 32, 24)
+    flag = pack_flag(dims, 21, 2.0, 5.0, 0.4)
+    out = []
+    for order in ("auto", "morton", "reference"):
+        with P.Simulation.from_flag(flag, *dims, tau=0.8, force=1e-4, precision="fp64",
+                                    ordering=order) as sim:
+            sim.init_dist_macro()
+            sim.step(5)
+            out.append((sim.get_f(), sim.macros()))
+    for f, m in out[1:]:
+        assert (f == out[0][0]).all() and all((a == b).all() for a, b in zip(m, out[0][1]))

@@ -178,5 +178,7 @@ def test_size_limits_rejected_before_any_device_work():
 
 def test_tuner_defaults_without_a_measurement():
     from porelb_gb300 import tune
-    assert tune.best("fp32", 12345) == dict(block_size=0, ordering="morton",
+    assert tune.best("fp32", 12345) == dict(block_size=0, ordering="auto",
                                             kernel_variant=0)
+    assert tune.best_pool("bf16dev") == dict(cta_threads=None, l2_prefetch=None,
+                                             ordering=None)
