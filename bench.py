@@ -37,9 +37,10 @@ BYTES_PER_NODE = {"fp64_exact": 376, "fp64": 376, "fp64_fma": 376, "fp32": 224,
 
 # DRAM bytes (read + write) of one step-kernel launch come from one-pass ncu
 # captures summarised in profiles/*.md, each with a line
-#   traffic-record: workload=W form=F num_node=N bytes=B source=D
-# where D is source_digest() of the step-kernel sources it was captured
-# from.  A record is reported only while the kernel sources are unchanged.
+#   traffic-record: workload=W form=F num_node=N order=O bytes=B source=D
+# where O is the node order of the run and D is source_digest() of the
+# step-kernel sources it was captured from.  A record is reported only
+# while the kernel sources are unchanged.
 PROFILES = os.path.join(ROOT, "profiles")
 STEP_SOURCES = ("plb_step.cu", "plb_fx.h", "plb_emu.h", "plb_internal.h")
 
@@ -53,7 +54,7 @@ def source_digest():
     return h.hexdigest()[:16]
 
 
-def recorded_traffic(workload, form, num_node):
+def recorded_traffic(workload, form, num_node, order):
     """(bytes, profile file) of the matching capture, or (None, reason)."""
     digest = source_digest()
     stale = None
@@ -69,8 +70,8 @@ def recorded_traffic(workload, form, num_node):
                 if not line.startswith("traffic-record:"):
                     continue
                 kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
-                if (kv.get("workload"), kv.get("form"), kv.get("num_node")) != \
-                        (workload, form, str(num_node)):
+                if (kv.get("workload"), kv.get("form"), kv.get("num_node"),
+                        kv.get("order")) != (workload, form, str(num_node), order):
                     continue
                 if kv.get("source") == digest:
                     return int(kv["bytes"]), "profiles/" + name
@@ -400,7 +401,8 @@ def run_gpu(args, rank, world, local):
         device=local, kernel_variant=kv))
 
     peak, peak_kind = hbm_peak()
-    traffic, traffic_src = recorded_traffic(args.workload, prec, N)
+    order = P.auto_ordering(N, dims[2], prec, local)
+    traffic, traffic_src = recorded_traffic(args.workload, prec, N, order)
     bpn = BYTES_PER_NODE[prec]
     achieved = bpn * N / (ms_step * 1e-3) / 1e9
     line = {
@@ -412,8 +414,7 @@ def run_gpu(args, rank, world, local):
         "data": DATA,
         "config": workload_config(args.workload, w, N, phi, prec),
         "parallelism": f"replicas{world}",
-        "layout": "SoA f[19][npad] ping-pong, %s node order"
-                  % P.auto_ordering(N, dims[2], prec, local),
+        "layout": "SoA f[19][npad] ping-pong, %s node order" % order,
         "k_darcy_after_run": kd, "steady_state": steady,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s",
