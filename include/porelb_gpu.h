@@ -78,9 +78,11 @@ enum {
  * warp's 32 consecutive nodes then have their neighbours in every direction
  * in one shifted run of nodes, which gathers best while the three z-planes
  * a step reads at once stay in L2.  MORTON keeps the gathers local at any
- * size.  AUTO takes REFERENCE when three z-planes of the domain's nodes fit
- * in half the L2, else MORTON (256^3: reference order, FP64 17.2 against
- * 16.4 GLUPS; 512^3 FP64 and 1024^3: Morton). */
+ * size.  AUTO takes REFERENCE when three z-planes of the domain's nodes
+ * (their distributions, words and numbering) fit in 60% of the L2, else
+ * MORTON
+ * (256^3: row order, FP64 17.2 against 16.4 GLUPS; 512^3 FP16 and FP32: row
+ * order; 512^3 and 1024^3 FP64: Morton). */
 enum { PLB_ORDER_MORTON = 0, PLB_ORDER_REFERENCE = 1, PLB_ORDER_AUTO = 2 };
 /* The order AUTO picks for n nodes in an nx*ny*nz domain with elem-byte
  * storage on device `device`. */

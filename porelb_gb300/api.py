@@ -143,8 +143,8 @@ def _params(tau, force, precision, ordering, halo, block_size, device,
 
 def auto_ordering(num_node, nz, precision, device=0):
     """The node order PLB_ORDER_AUTO picks for this domain and form:
-    "reference" (row order) when three z-planes of its nodes fit in half the
-    L2, else "morton"."""
+    "reference" (row order) when three z-planes of its nodes fit in 60% of
+    the L2, else "morton"."""
     elem = {"fp64_exact": 8, "fp64": 8, "fp64_fma": 8, "fp32": 4, "fp16dev": 2,
             "bf16dev": 2}[precision]
     o = _lib.load().plb_auto_ordering(int(num_node), int(nz), elem, device)

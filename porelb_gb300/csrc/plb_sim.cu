@@ -76,7 +76,10 @@ int plb_auto_ordering(long long n, int nz, int elem_bytes, int device)
         l2 <= 0)
         return PLB_ORDER_MORTON;
     const double plane = bpn * (double)n / nz;
-    return 3.0 * plane <= 0.5 * (double)l2 ? PLB_ORDER_REFERENCE : PLB_ORDER_MORTON;
+    /* measured: row order wins up to about 63 MB of such planes on a 126 MB
+     * L2 (512^3 FP32) and loses from 105 MB (512^3 FP64, whose L2 prefetch
+     * also takes room) */
+    return 3.0 * plane <= 0.6 * (double)l2 ? PLB_ORDER_REFERENCE : PLB_ORDER_MORTON;
 }
 
 /* ------------------------------------------------------ allocation */
@@ -282,6 +285,14 @@ __global__ void k_morton_mark(const plb_node_info *V, int n, int nx, int ny,
     }
     const uint64_t c = morton3(r.x, r.y, r.z, b);
     atomicOr(bitmap + (c >> 5), 1u << (c & 31));
+}
+
+/* a node number the Morton numbering left unassigned: two records on one
+ * cell */
+__global__ void k_perm_holes(const int *perm, int n, unsigned *bad)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && perm[k] < 0) atomicOr(bad, kDupCoord);
 }
 
 __global__ void k_popc(const uint32_t *bitmap, uint32_t *cnt, size_t m)
@@ -623,7 +634,14 @@ static int build_tables(plb_sim *s, const plb_node_info *V_host)
     CKT(cudaMemcpyAsync(dstart, s->v_sub_start, sizeof(int) * (size_t)(s->num_p + 1),
                         cudaMemcpyHostToDevice, st));
     CKT(cudaMemsetAsync(s->perm, 0xff, sizeof(int) * (size_t)s->npad, st));
-    if (s->ordering == PLB_ORDER_MORTON && n > 0) {
+    /* The Morton pass also validates the records (coordinates inside the
+     * box, no two nodes on one cell: a repeated cell leaves a hole in the
+     * numbering), so it runs for every order; in row order its numbering
+     * is then replaced by the identity. */
+    if (n > 0 && ceil_log2(s->nx) + ceil_log2(s->ny) + ceil_log2(s->nz) > 40 &&
+        s->ordering == PLB_ORDER_REFERENCE) {
+        k_identity<<<nblk(n, 256), 256, 0, st>>>(s->perm, inv, n);
+    } else if (n > 0) {
         MortonBits b{ceil_log2(s->nx), ceil_log2(s->ny), ceil_log2(s->nz)};
         const int bits = b.bx + b.by + b.bz;
         if (bits > 40) {
@@ -644,8 +662,10 @@ static int build_tables(plb_sim *s, const plb_node_info *V_host)
         if (rc != PLB_OK) goto done;
         k_morton_assign<<<nblk(n, 256), 256, 0, st>>>(dV, n, s->nx, s->ny, s->nz, b, bitmap,
                                                      offs, s->perm, inv, bad);
-    } else if (n > 0) {
-        k_identity<<<nblk(n, 256), 256, 0, st>>>(s->perm, inv, n);
+        if (s->ordering != PLB_ORDER_MORTON) {
+            k_perm_holes<<<nblk(n, 256), 256, 0, st>>>(s->perm, n, bad);
+            k_identity<<<nblk(n, 256), 256, 0, st>>>(s->perm, inv, n);
+        }
     }
     CKT(cudaGetLastError());
     if (n > 0) {
