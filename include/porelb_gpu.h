@@ -135,7 +135,7 @@ typedef struct plb_sim plb_sim;
 /* ---------------------------------------------------------------- tables */
 
 /* Fill *p with the reference defaults: tau 0.8, force 1e-3 (init_para,
- * porelb.c:83-94), FP64_EXACT, Morton order, automatic halo semantics. */
+ * porelb.c:83-94), FP64_EXACT, automatic node order and halo semantics. */
 void plb_default_params(plb_params *p);
 
 /* Replaces build_V (preprocess.c:29-164).  flag is nx*ny*nz uint8, x fastest,
