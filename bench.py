@@ -548,8 +548,8 @@ def run_pool(args):
 def batched_result(n_samples, K, max_steps, plain_steps):
     """The batched workload (n_samples samples of seed 3, FP32 storage, each
     to its 1e-7 steady-state test) in one pool, against looping the plain
-    FP32 kernel over the samples, with each sample's permeability against
-    the FP64 pool's."""
+    FP32 kernel and the plain FP64 form over the samples, with each
+    sample's permeability against the FP64 pool's."""
     import torch
     import porelb_gb300 as P
     from porelb_gb300.workloads import batched_samples
@@ -560,22 +560,28 @@ def batched_result(n_samples, K, max_steps, plain_steps):
               for f in ("fp32", "fp64")}
     res32, ns32, wall32 = _steady_batch(samples, "fp32", K, max_steps)
     res64, ns64, wall64 = _steady_batch(samples, "fp64", K, max_steps)
-    # plain kernel per sample (FP32), timed on a fixed step count, then the
-    # loop over samples is costed with each sample's own step count
+    # plain kernel per sample (FP32, and the FP64 plain form), timed on a
+    # fixed step count, then each loop over the samples is costed with each
+    # sample's own step count in its pool
     loop_s = 0.0
+    loop64_s = 0.0
     for smp in samples:
-        sim = P.Simulation.packed(smp.seed, smp.edge, smp.edge, smp.edge,
-                                  smp.rmin, smp.rmax, smp.porosity,
-                                  tau=smp.tau, force=smp.force,
-                                  precision="fp32")
-        sim.init_dist_macro()
-        sim.step(20)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sim.step(plain_steps, it_begin=20)
-        el = time.perf_counter() - t0
-        sim.close()
-        loop_s += el / plain_steps * res32[smp.index]["steps"]
+        for prec in ("fp32", "fp64"):
+            sim = P.Simulation.packed(smp.seed, smp.edge, smp.edge, smp.edge,
+                                      smp.rmin, smp.rmax, smp.porosity,
+                                      tau=smp.tau, force=smp.force,
+                                      precision=prec)
+            sim.init_dist_macro()
+            sim.step(20)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sim.step(plain_steps, it_begin=20)
+            el = time.perf_counter() - t0
+            sim.close()
+            if prec == "fp32":
+                loop_s += el / plain_steps * res32[smp.index]["steps"]
+            else:
+                loop64_s += el / plain_steps * res64[smp.index]["steps"]
     errs = [abs(res32[i]["k_darcy"] - res64[i]["k_darcy"]) /
             abs(res64[i]["k_darcy"]) for i in res32 if res64[i]["k_darcy"]]
     conv = sum(1 for r in res32.values() if r["status"] == 1)
@@ -584,6 +590,9 @@ def batched_result(n_samples, K, max_steps, plain_steps):
         "value": round(ns32 / wall32 / 1e6, 1), "unit": "MLUPS",
         "plain_loop_mlups": round(ns32 / loop_s / 1e6, 1),
         "speedup_vs_plain_loop": round(loop_s / wall32, 3),
+        # the plain form (FP64, one sample at a time) on the same samples
+        "plain_fp64_loop_mlups": round(ns64 / loop64_s / 1e6, 1),
+        "mlups_ratio_vs_plain_fp64_loop": round((ns32 / wall32) / (ns64 / loop64_s), 3),
         "fp64_batched_mlups": round(ns64 / wall64 / 1e6, 1),
         "samples": len(samples), "converged": conv,
         "k_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs),
@@ -612,6 +621,7 @@ def _plain_fp64_fcfs(reqs, K, max_steps):
     import torch
     import porelb_gb300 as P
     ks, service = {}, []
+    node_steps, stepping_s = 0, 0.0
     for r in reqs:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -621,9 +631,12 @@ def _plain_fp64_fcfs(reqs, K, max_steps):
         sim.init_dist_macro()
         it, prev, k, checks = 0, None, None, 0
         while it < max_steps:
+            ts = time.perf_counter()
             sim.step(K, it_begin=it)
             it += K
             k = sim.permeability()[0]
+            stepping_s += time.perf_counter() - ts
+            node_steps += sim.N * K
             checks += 1
             if checks >= 2 and k != 0 and abs(k - prev) <= r.tol * abs(k):
                 break
@@ -640,7 +653,9 @@ def _plain_fp64_fcfs(reqs, K, max_steps):
     return ks, dict(solves_per_s=len(reqs) / span if span > 0 else None,
                     p50_latency_s=float(np.percentile(lat, 50)),
                     p99_latency_s=float(np.percentile(lat, 99)),
-                    mean_solve_s=float(np.mean(service)))
+                    mean_solve_s=float(np.mean(service)),
+                    fluid_mlups_stepping=(node_steps / stepping_s / 1e6
+                                          if stepping_s > 0 else None))
 
 
 SERVE_FORMS = {"fp16dev": "FP16 deviations", "bf16dev": "BF16 deviations",
@@ -672,6 +687,9 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
         served = [r for r in reqs if r.index in by]
         ks64, plain = _plain_fp64_fcfs(served, K, max_steps)
         perr = [abs(by[i]["k_darcy"] - k) / abs(k) for i, k in ks64.items() if k]
+        if plain["fluid_mlups_stepping"] and summ["fluid_mlups_busy"]:
+            plain["mlups_ratio_served_busy_vs_plain_fp64"] = round(
+                summ["fluid_mlups_busy"] / plain["fluid_mlups_stepping"], 3)
         plain["k_rel_err_served_vs_plain_fp64"] = {
             "max": max(perr) if perr else None,
             "median": statistics.median(perr) if perr else None,
@@ -682,6 +700,8 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
         "p50_latency_s": round(summ["p50_latency_s"], 3),
         "p99_latency_s": round(summ["p99_latency_s"], 3),
         "fluid_mlups": round(summ["fluid_mlups"], 1),
+        "fluid_mlups_gpu_busy": (round(summ["fluid_mlups_busy"], 1)
+                                 if summ["fluid_mlups_busy"] else None),
         "requests_done": summ["requests"], "requests": len(reqs),
         "rejected": len(summ["rejected"]),
         "k_rel_err_vs_fp64": {"checked": len(errs),

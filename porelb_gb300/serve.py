@@ -210,6 +210,8 @@ class Server:
                        p50_latency_s=float(np.percentile(lat, 50)),
                        p99_latency_s=float(np.percentile(lat, 99)),
                        fluid_mlups=node_steps / wall / 1e6 if wall > 0 else 0.0,
+                       fluid_mlups_busy=(node_steps / (busy_ms / 1e3) / 1e6
+                                         if busy_ms > 0 else None),
                        intervals=rounds, capacity_nodes=self.capacity,
                        admit_s=t_admit, wait_s=t_wait,
                        gpu_busy_s=busy_ms / 1e3,
