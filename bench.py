@@ -522,7 +522,11 @@ def run_pool(args):
     torch.cuda.set_device(0)
     K = args.check_every
     cap = int(args.samples * (args.edge ** 3 * 0.40 + 512))
-    b = Batch(cap, max(args.samples, 1), args.precision, check_every=K)
+    groups = {"off": False, "l2": True}.get(args.l2_groups)
+    if groups is None:
+        groups = int(args.l2_groups)
+    b = Batch(cap, max(args.samples, 1), args.precision, check_every=K,
+              l2_groups=groups)
     n = 0
     for k in range(args.samples):
         sid = b.add_packed(100 + k, args.edge, args.edge, args.edge, 3.0, 6.0, 0.35,
@@ -541,7 +545,8 @@ def run_pool(args):
             "steps": intervals * K, "num_node": n,
             "config": {"workload": f"pool of {args.samples} sphere packs of "
                                    f"{args.edge}^3, seeds 100+",
-                       "check_every": K, "precision": args.precision}}
+                       "check_every": K, "precision": args.precision,
+                       "l2_groups": args.l2_groups}}
     print(json.dumps(line), flush=True)
 
 
@@ -844,6 +849,9 @@ def main():
                     help="also serve the same requests with the FP64 plain "
                          "form, one at a time (first come first served)")
     ap.add_argument("--edge", type=int, default=1024)
+    ap.add_argument("--l2-groups", default="off",
+                    help="pool mode: the pool's L2 groups (off, l2 = 60%% of "
+                         "the L2, or a budget in KiB)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the served and batched runs of the default line")
     ap.add_argument("--extra-requests", type=int, default=200,

@@ -306,7 +306,15 @@ typedef struct {
                               PLB_ORDER_MORTON (0, default),
                               PLB_ORDER_REFERENCE or PLB_ORDER_AUTO (chosen
                               per sample) */
-    int reserved[5];
+    int l2_group_kb;       /* L2 groups: samples whose working set (both
+                              distribution buffers and the neighbour words)
+                              fits this many KiB are packed into groups, and
+                              an interval runs its K steps one group at a
+                              time while the group stays in L2; larger
+                              samples step together first.  0 = off (the
+                              default), -1 = 60% of the device's L2.  Results
+                              are the same bits either way. */
+    int reserved[4];
 } plb_batch_params;
 int plb_batch_create_ex(const plb_batch_params *p, plb_batch **out);
 void plb_batch_destroy(plb_batch *b);

@@ -54,7 +54,8 @@ class BatchParams(ctypes.Structure):
                 ("precision", ctypes.c_int), ("check_every", ctypes.c_int),
                 ("keep_macros", ctypes.c_int), ("device", ctypes.c_int),
                 ("cta_threads", ctypes.c_int), ("l2_prefetch", ctypes.c_int),
-                ("ordering", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("ordering", ctypes.c_int), ("l2_group_kb", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 _P = ctypes.c_void_p

@@ -21,11 +21,14 @@ PARKED = 4
 class Batch:
     def __init__(self, capacity_nodes, max_samples=1024, precision="fp32",
                  check_every=1000, keep_macros=False, device=0, cta_threads=None,
-                 l2_prefetch=None, ordering=None):
+                 l2_prefetch=None, ordering=None, l2_groups=None):
         """cta_threads (128 or 256), l2_prefetch (True/False) and ordering
         ("morton" or "reference"): the batch step's launch and the samples'
         node order; None takes the launch tuner's cached choice for this
-        form (porelb_gb300.tune.tune_pool), else the library default."""
+        form (porelb_gb300.tune.tune_pool), else the library default.
+        l2_groups: L2 groups of the samples that fit a budget (each group
+        steps its interval while it stays in L2): None or False = off,
+        True = 60% of the L2, or a budget in KiB."""
         self._lib = _lib.load()
         self.precision = precision
         self.check_every = check_every
@@ -48,6 +51,8 @@ class Batch:
         bp.cta_threads = int(cta_threads or 0)
         bp.l2_prefetch = 0 if l2_prefetch is None else (1 if l2_prefetch else -1)
         bp.ordering = ORDERINGS[ordering or "auto"]
+        bp.l2_group_kb = (0 if l2_groups is None or l2_groups is False else
+                          (-1 if l2_groups is True else int(l2_groups)))
         h = ctypes.c_void_p()
         _check(self._lib.plb_batch_create_ex(ctypes.byref(bp), ctypes.byref(h)),
                "plb_batch_create_ex")

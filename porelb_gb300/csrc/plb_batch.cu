@@ -6,10 +6,13 @@
  * scale the step applies (k_batch_step, plb_step.cu).  All samples advance
  * together: one launch per lattice step covers every active block, and an
  * interval of K steps (the last writing the per-block sums) plus the
- * per-sample reduction is one CUDA graph, built once and replayed;
+ * per-sample reduction are CUDA graphs, built once and replayed;
  * admissions and retirements only change the active-block list and the
- * grid of the step nodes.  An interval is launched asynchronously
- * (plb_batch_launch) and completed by plb_batch_finish, which checks each
+ * grid of the step nodes.  On request (l2_group_kb) the samples that fit
+ * a budget are packed into L2 groups, and the interval steps each group
+ * K times while it stays in L2, replaying one group chain per group.  An
+ * interval is launched asynchronously (plb_batch_launch) and completed by
+ * plb_batch_finish, which checks each
  * sample's steady-state criterion (relative change of the mean u_x over
  * the interval), retires converged samples and frees their blocks.
  * Samples admitted while an interval runs are built on a second stream into
@@ -276,12 +279,27 @@ struct plb_batch {
     std::map<long long, long long> free_blocks; /* start -> length */
     std::vector<SampleHost> s;
     std::vector<int> done;
+    /* K steps over the blocks of the samples outside the L2 groups */
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int graph_cur = -1;
     int graph_grid = 0;                     /* grid of the step nodes */
     std::vector<BatchArgs> step_args;       /* kernel arguments per step node */
     std::vector<cudaGraphNode_t> step_nodes;
+    /* L2 groups: samples whose working set fits group_bytes are packed into
+     * groups, and the interval steps one group K times while it stays in
+     * L2, then the next (0 = no groups) */
+    size_t group_bytes = 0;
+    std::vector<int> hgroups;               /* {first list entry, blocks} */
+    int *dgroups = nullptr;                 /* device copy */
+    int *gcur = nullptr;                    /* device: the group being stepped */
+    int big_blocks = 0, group_blocks_max = 0;
+    cudaGraph_t graph_grp = nullptr;        /* K steps of group *gcur, then ++*gcur */
+    cudaGraphExec_t gexec_grp = nullptr;
+    int grp_grid = 0;
+    std::vector<BatchArgs> grp_args;
+    std::vector<cudaGraphNode_t> grp_nodes;
+    cudaGraphExec_t gexec_tail = nullptr;   /* step counter, sums, read-back */
     size_t bytes = 0;
 };
 
@@ -308,6 +326,11 @@ static void batch_free(plb_batch *b)
     if (!b) return;
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->gexec_grp) cudaGraphExecDestroy(b->gexec_grp);
+    if (b->graph_grp) cudaGraphDestroy(b->graph_grp);
+    if (b->gexec_tail) cudaGraphExecDestroy(b->gexec_tail);
+    cudaFree(b->dgroups);
+    cudaFree(b->gcur);
     cudaFree(b->f[0]);
     cudaFree(b->f[1]);
     cudaFree(b->nbr);
@@ -364,7 +387,7 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     const int check_every = bp->check_every, keep_macros = bp->keep_macros;
     const int device = bp->device;
     if ((bp->cta_threads != 0 && bp->cta_threads != 128 && bp->cta_threads != B) ||
-        bp->l2_prefetch < -1 || bp->l2_prefetch > 1 ||
+        bp->l2_prefetch < -1 || bp->l2_prefetch > 1 || bp->l2_group_kb < -1 ||
         (bp->ordering != PLB_ORDER_MORTON && bp->ordering != PLB_ORDER_REFERENCE &&
          bp->ordering != PLB_ORDER_AUTO))
         return PLB_ERR_ARG;
@@ -386,6 +409,18 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     b->cta = bp->cta_threads ? bp->cta_threads : batch_default_cta(precision);
     b->ordering = bp->ordering;
     b->prefetch = bp->l2_prefetch > 0 || (bp->l2_prefetch == 0 && precision == PLB_FP64);
+    /* L2 groups on request: a budget in KiB, or -1 for 60% of the L2.  They
+     * pay for pools of samples that fit in L2 (FP32 pools of 64^3 and 96^3
+     * packs step 1.1-1.14x faster); on the batched workload, whose time goes
+     * to samples larger than L2, they gained 1% of device time and cost
+     * more than that in graph building */
+    if (bp->l2_group_kb > 0) {
+        b->group_bytes = (size_t)bp->l2_group_kb * 1024;
+    } else if (bp->l2_group_kb == -1) {
+        int l2 = 0;
+        if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device) == cudaSuccess && l2 > 0)
+            b->group_bytes = (size_t)l2 * 3 / 5;
+    }
     b->cap_blocks = (long long)((capacity_nodes + B - 1) / B);
     b->rest = b->cap_blocks * B;
     b->npad = b->rest + B;
@@ -414,6 +449,8 @@ int plb_batch_create_ex(const plb_batch_params *bp, plb_batch **out)
     al(&b->ssum, 8 * 3 * (size_t)max_samples);
     al(&b->serr, 4 * (size_t)max_samples);
     al(&b->t_dev, 4);
+    al(&b->dgroups, 4 * 2 * (size_t)max_samples);
+    al(&b->gcur, 4);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_ssum, 8 * 3 * (size_t)max_samples);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_serr, 4 * (size_t)max_samples);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->blk, 0xff, 4 * (size_t)b->cap_blocks, b->st);
@@ -598,21 +635,13 @@ int plb_batch_add_packed(plb_batch *b, uint64_t seed, int nx, int ny, int nz,
     return rc;
 }
 
-/* Build the interval graph: K batch-step kernel nodes in a chain (the last
- * writes the sums), the step counter advance, the per-sample reduction and
- * its read-back.  The step nodes' grid is the active-block count; when the
- * active list changes only their grid is updated (set_graph_grid), so
- * admissions and retirements never rebuild the graph. */
-static int build_graph(plb_batch *b)
+/* A chain of K batch-step kernel nodes (the last writes the sums) from
+ * buffer cur, over `grid` CTAs; with `grouped` the launches step the L2
+ * group *gcur and a last node moves *gcur to the next group. */
+static cudaError_t step_chain(plb_batch *b, bool grouped, int grid,
+                              std::vector<BatchArgs> &args,
+                              std::vector<cudaGraphNode_t> &nodes, cudaGraph_t *out)
 {
-    if (b->gexec) {
-        cudaGraphExecDestroy(b->gexec);
-        b->gexec = nullptr;
-    }
-    if (b->graph) {
-        cudaGraphDestroy(b->graph);
-        b->graph = nullptr;
-    }
     BatchArgs a;
     memset(&a, 0, sizeof(a));
     a.nbr = b->nbr;
@@ -628,17 +657,21 @@ static int build_graph(plb_batch *b)
     a.macro = b->macro;
     a.partial = b->partial;
     a.serr = b->serr;
+    if (grouped) {
+        a.grp = b->dgroups;
+        a.grp_cur = b->gcur;
+    }
     const int bt = b->cta;
     const void *fn = batch_step_kernel(b->precision, false, bt);
     const void *fn_m = batch_step_kernel(b->precision, true, bt);
-    b->step_args.assign((size_t)b->K, a);
-    b->step_nodes.assign((size_t)b->K, nullptr);
-    b->graph_grid = (int)b->hlist.size() * h;
-    cudaError_t e = cudaGraphCreate(&b->graph, 0);
+    args.assign((size_t)b->K, a);
+    nodes.assign((size_t)b->K, nullptr);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
     cudaGraphNode_t prev = nullptr;
     int cur = b->cur;
     for (int k = 0; k < b->K && e == cudaSuccess; k++) {
-        BatchArgs &ak = b->step_args[(size_t)k];
+        BatchArgs &ak = args[(size_t)k];
         ak.fin = b->f[cur];
         ak.fout = b->f[cur ^ 1];
         ak.t_off = k;
@@ -647,13 +680,60 @@ static int build_graph(plb_batch *b)
         cudaKernelNodeParams p;
         memset(&p, 0, sizeof(p));
         p.func = (void *)(k == b->K - 1 ? fn_m : fn);
-        p.gridDim = dim3((unsigned)(b->graph_grid > 0 ? b->graph_grid : 1));
+        p.gridDim = dim3((unsigned)(grid > 0 ? grid : 1));
         p.blockDim = dim3((unsigned)bt);
         p.kernelParams = kp;
-        e = cudaGraphAddKernelNode(&b->step_nodes[(size_t)k], b->graph, prev ? &prev : nullptr,
+        e = cudaGraphAddKernelNode(&nodes[(size_t)k], g, prev ? &prev : nullptr,
                                    prev ? 1 : 0, &p);
-        prev = b->step_nodes[(size_t)k];
+        prev = nodes[(size_t)k];
     }
+    if (grouped && e == cudaSuccess) {
+        int *gc = b->gcur;
+        int one = 1;
+        void *kp[2] = {&gc, &one};
+        cudaKernelNodeParams p;
+        memset(&p, 0, sizeof(p));
+        p.func = (void *)k_advance;
+        p.gridDim = dim3(1);
+        p.blockDim = dim3(1);
+        p.kernelParams = kp;
+        cudaGraphNode_t n = nullptr;
+        e = cudaGraphAddKernelNode(&n, g, &prev, 1, &p);
+    }
+    if (e != cudaSuccess && g) {
+        cudaGraphDestroy(g);
+        g = nullptr;
+    }
+    *out = g;
+    return e;
+}
+
+/* Build the interval graphs: the K-step chain over the samples outside the
+ * L2 groups, the K-step chain of one group (replayed once per group), and
+ * the tail: the step counter advance, the per-sample reduction and its
+ * read-back.  The chains' grid follows the active list; when it changes
+ * only the grid is updated (set_graph_grid), so admissions and retirements
+ * never rebuild the graphs. */
+static int build_graph(plb_batch *b)
+{
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->gexec_grp) cudaGraphExecDestroy(b->gexec_grp);
+    if (b->graph_grp) cudaGraphDestroy(b->graph_grp);
+    if (b->gexec_tail) cudaGraphExecDestroy(b->gexec_tail);
+    b->gexec = b->gexec_grp = b->gexec_tail = nullptr;
+    b->graph = b->graph_grp = nullptr;
+    const int h = B / b->cta;
+    b->graph_grid = b->big_blocks * h;
+    b->grp_grid = b->group_blocks_max * h;
+    cudaError_t e = step_chain(b, false, b->graph_grid, b->step_args, b->step_nodes, &b->graph);
+    if (e == cudaSuccess)
+        e = step_chain(b, true, b->grp_grid, b->grp_args, b->grp_nodes, &b->graph_grp);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, b->graph, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec_grp, b->graph_grp, 0);
+    cudaGraph_t tail = nullptr;
+    if (e == cudaSuccess) e = cudaGraphCreate(&tail, 0);
+    cudaGraphNode_t prev = nullptr;
     int *t_dev = b->t_dev;
     int K = b->K;
     if (e == cudaSuccess) {
@@ -664,9 +744,7 @@ static int build_graph(plb_batch *b)
         p.gridDim = dim3(1);
         p.blockDim = dim3(1);
         p.kernelParams = kp;
-        cudaGraphNode_t n = nullptr;
-        e = cudaGraphAddKernelNode(&n, b->graph, &prev, 1, &p);
-        prev = n;
+        e = cudaGraphAddKernelNode(&prev, tail, nullptr, 0, &p);
     }
     const SampleDev *sd = b->sdev;
     const int *sa = b->sactive;
@@ -683,21 +761,22 @@ static int build_graph(plb_batch *b)
         p.blockDim = dim3(128);
         p.kernelParams = kp;
         cudaGraphNode_t n = nullptr;
-        e = cudaGraphAddKernelNode(&n, b->graph, &prev, 1, &p);
+        e = cudaGraphAddKernelNode(&n, tail, &prev, 1, &p);
         prev = n;
     }
     if (e == cudaSuccess) {
         cudaGraphNode_t n = nullptr;
-        e = cudaGraphAddMemcpyNode1D(&n, b->graph, &prev, 1, b->h_ssum, b->ssum,
+        e = cudaGraphAddMemcpyNode1D(&n, tail, &prev, 1, b->h_ssum, b->ssum,
                                      8 * 3 * (size_t)b->max_samples, cudaMemcpyDeviceToHost);
         prev = n;
     }
     if (e == cudaSuccess) {
         cudaGraphNode_t n = nullptr;
-        e = cudaGraphAddMemcpyNode1D(&n, b->graph, &prev, 1, b->h_serr, b->serr,
+        e = cudaGraphAddMemcpyNode1D(&n, tail, &prev, 1, b->h_serr, b->serr,
                                      4 * (size_t)b->max_samples, cudaMemcpyDeviceToHost);
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, b->graph, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->gexec_tail, tail, 0);
+    if (tail) cudaGraphDestroy(tail);
     if (e != cudaSuccess) {
         fprintf(stderr, "porelb_gpu: batch graph build failed: %s\n", cudaGetErrorString(e));
         return PLB_ERR_CUDA;
@@ -706,28 +785,109 @@ static int build_graph(plb_batch *b)
     return PLB_OK;
 }
 
-/* The step nodes of the instantiated graph get the current active-block
- * count as their grid. */
-static int set_graph_grid(plb_batch *b)
+/* Set the grid of the step nodes of one chain. */
+static int set_chain_grid(plb_batch *b, cudaGraphExec_t exec, std::vector<BatchArgs> &args,
+                          std::vector<cudaGraphNode_t> &nodes, int grid)
 {
-    const int h = B / b->cta;
-    const int grid = (int)b->hlist.size() * h;
-    if (grid == b->graph_grid || grid == 0) return PLB_OK;
     const int bt = b->cta;
     const void *fn = batch_step_kernel(b->precision, false, bt);
     const void *fn_m = batch_step_kernel(b->precision, true, bt);
     for (int k = 0; k < b->K; k++) {
-        void *kp[1] = {&b->step_args[(size_t)k]};
+        void *kp[1] = {&args[(size_t)k]};
         cudaKernelNodeParams p;
         memset(&p, 0, sizeof(p));
         p.func = (void *)(k == b->K - 1 ? fn_m : fn);
         p.gridDim = dim3((unsigned)grid);
         p.blockDim = dim3((unsigned)bt);
         p.kernelParams = kp;
-        BCK(cudaGraphExecKernelNodeSetParams(b->gexec, b->step_nodes[(size_t)k], &p));
+        BCK(cudaGraphExecKernelNodeSetParams(exec, nodes[(size_t)k], &p));
     }
-    b->graph_grid = grid;
     return PLB_OK;
+}
+
+/* The chains of the instantiated graphs get the current block counts as
+ * their grids: the samples outside the groups, and the largest group. */
+static int set_graph_grid(plb_batch *b)
+{
+    const int h = B / b->cta;
+    const int grid = b->big_blocks * h;
+    if (grid != b->graph_grid && grid > 0) {
+        const int rc = set_chain_grid(b, b->gexec, b->step_args, b->step_nodes, grid);
+        if (rc != PLB_OK) return rc;
+        b->graph_grid = grid;
+    }
+    const int ggrid = b->group_blocks_max * h;
+    if (ggrid != b->grp_grid && ggrid > 0) {
+        const int rc = set_chain_grid(b, b->gexec_grp, b->grp_args, b->grp_nodes, ggrid);
+        if (rc != PLB_OK) return rc;
+        b->grp_grid = ggrid;
+    }
+    return PLB_OK;
+}
+
+/* The active pool blocks in the order the interval steps them: first the
+ * samples that step outside the L2 groups, then the groups.  Samples whose
+ * working set fits group_bytes are packed first fit, largest first, into
+ * groups of at most group_bytes; since one chain with the largest group's
+ * grid steps every group, a group below half the largest one's blocks
+ * (mostly empty CTAs) steps with the samples outside the groups instead. */
+static void order_blocks(plb_batch *b)
+{
+    std::vector<std::pair<long long, int>> order;
+    for (int sid = 0; sid < b->max_samples; sid++)
+        if (b->s[sid].active) order.emplace_back(b->s[sid].blk0, sid);
+    std::sort(order.begin(), order.end());
+    const size_t per_block = (size_t)B * (2 * Q * b->elem + 72);
+    std::vector<int> small;
+    std::vector<char> grouped((size_t)b->max_samples, 0);
+    if (b->group_bytes > 0)
+        for (auto &o : order)
+            if ((size_t)b->s[o.second].nblk * per_block <= b->group_bytes)
+                small.push_back(o.second);
+    std::stable_sort(small.begin(), small.end(), [&](int x, int y) {
+        return b->s[x].nblk > b->s[y].nblk;
+    });
+    std::vector<std::vector<int>> bins;
+    std::vector<size_t> used;
+    for (int sid : small) {
+        const size_t need = (size_t)b->s[sid].nblk * per_block;
+        size_t k = 0;
+        while (k < bins.size() && used[k] + need > b->group_bytes) k++;
+        if (k == bins.size()) {
+            bins.emplace_back();
+            used.push_back(0);
+        }
+        bins[k].push_back(sid);
+        used[k] += need;
+    }
+    size_t biggest = 0;
+    for (size_t u : used) biggest = std::max(biggest, u);
+    for (size_t k = 0; k < bins.size(); k++)
+        if (2 * used[k] >= biggest)
+            for (int sid : bins[k]) grouped[(size_t)sid] = 1;
+    b->hlist.clear();
+    b->hgroups.clear();
+    for (auto &o : order) {
+        const SampleHost &h = b->s[o.second];
+        if (grouped[(size_t)o.second]) continue;
+        for (long long k = 0; k < h.nblk; k++) b->hlist.push_back((int)(h.blk0 + k));
+    }
+    b->big_blocks = (int)b->hlist.size();
+    b->group_blocks_max = 0;
+    for (size_t k = 0; k < bins.size(); k++) {
+        if (2 * used[k] < biggest) continue;
+        std::vector<int> members = bins[k];
+        std::sort(members.begin(), members.end(),
+                  [&](int x, int y) { return b->s[x].blk0 < b->s[y].blk0; });
+        const int first = (int)b->hlist.size();
+        for (int sid : members)
+            for (long long q = 0; q < b->s[sid].nblk; q++)
+                b->hlist.push_back((int)(b->s[sid].blk0 + q));
+        const int cnt = (int)b->hlist.size() - first;
+        b->hgroups.push_back(first);
+        b->hgroups.push_back(cnt);
+        b->group_blocks_max = std::max(b->group_blocks_max, cnt);
+    }
 }
 
 /* The sample stops being stepped: it leaves the active list and its
@@ -770,18 +930,12 @@ int plb_batch_launch(plb_batch *b, int *n_active)
         h.stepping = h.active;
     }
     if (b->list_dirty) {
-        /* the pool blocks of the active samples, in pool order */
-        std::vector<std::pair<long long, int>> order;
-        for (int sid = 0; sid < b->max_samples; sid++)
-            if (b->s[sid].active) order.emplace_back(b->s[sid].blk0, sid);
-        std::sort(order.begin(), order.end());
-        b->hlist.clear();
-        for (auto &o : order) {
-            const SampleHost &h = b->s[o.second];
-            for (long long k = 0; k < h.nblk; k++) b->hlist.push_back((int)(h.blk0 + k));
-        }
+        order_blocks(b);
         if (!b->hlist.empty())
             BCK(cudaMemcpyAsync(b->blist, b->hlist.data(), 4 * b->hlist.size(),
+                                cudaMemcpyHostToDevice, b->st));
+        if (!b->hgroups.empty())
+            BCK(cudaMemcpyAsync(b->dgroups, b->hgroups.data(), 4 * b->hgroups.size(),
                                 cudaMemcpyHostToDevice, b->st));
         b->list_dirty = false;
     }
@@ -793,7 +947,13 @@ int plb_batch_launch(plb_batch *b, int *n_active)
         if (rc != PLB_OK) return rc;
     }
     BCK(cudaEventRecord(b->ev0, b->st));
-    BCK(cudaGraphLaunch(b->gexec, b->st));
+    if (b->big_blocks > 0) BCK(cudaGraphLaunch(b->gexec, b->st));
+    const int ngroups = (int)(b->hgroups.size() / 2);
+    if (ngroups > 0) {
+        BCK(cudaMemsetAsync(b->gcur, 0, 4, b->st));
+        for (int g = 0; g < ngroups; g++) BCK(cudaGraphLaunch(b->gexec_grp, b->st));
+    }
+    BCK(cudaGraphLaunch(b->gexec_tail, b->st));
     BCK(cudaEventRecord(b->ev1, b->st));
     b->in_flight = true;
     return PLB_OK;

@@ -120,6 +120,10 @@ struct BatchArgs {
                                   max |stored deviation| */
     unsigned int *serr;        /* per-sample error bits */
     int pf_blocks;             /* L2 prefetch distance in CTAs (0 = none) */
+    /* L2 groups: when grp is set, the launch steps group *grp_cur only,
+     * pool blocks blk_list[grp[2g] .. grp[2g] + grp[2g + 1]) */
+    const int *grp;
+    const int *grp_cur;
 };
 
 /* Exclusive scan of m uint32 counts into offs (device memory). */

@@ -486,8 +486,9 @@ k_step(const StepArgs a)
 }
 
 /* Batch step: kBatchBlock / BT CTAs of BT threads per active pool block;
- * CTA b works on part b % H of pool block blk_list[b / H], whose map entry
- * blk_sample[] packs its sample and that sample's node count in it.  CTAs
+ * CTA b works on part b % H of pool block blk_list[b / H] (of the current
+ * L2 group's window of the list, when the pool steps in groups), whose map
+ * entry blk_sample[] packs its sample and that sample's node count in it.  CTAs
  * that run at the same time work on neighbouring pool blocks, so in Morton
  * order their gathers share L2 lines (a fixed grid looping over the list
  * lost that and ran 23% slower in the FP64 form). */
@@ -497,18 +498,27 @@ k_batch_step(const BatchArgs a)
 {
     using T = typename StoreOf<PREC>::T;
     constexpr int H = kBatchBlock / BT; /* CTAs per pool block */
+    const int *list = a.blk_list;
+    int ncta = (int)gridDim.x;
+    if (a.grp) {
+        /* one L2 group of the interval: its window of the block list */
+        const int g = *a.grp_cur;
+        list += a.grp[2 * g];
+        ncta = a.grp[2 * g + 1] * H;
+        if ((int)blockIdx.x >= ncta) return;
+    }
     const int part = blockIdx.x % H;
-    const int pb = a.blk_list[blockIdx.x / H];
+    const int pb = list[blockIdx.x / H];
     const int packed = a.blk_sample[pb];
     const int s = packed >> 9;                  /* -1: free block */
     const int k = part * BT + threadIdx.x;      /* node within the pool block */
     const bool valid = s >= 0 && k < (packed & 511);
     const long long i = (long long)pb * kBatchBlock + k;
     /* L2 prefetch of the part of a pool block the CTA pf_blocks later steps */
-    if (a.pf_blocks > 0 && threadIdx.x == 0 && blockIdx.x + a.pf_blocks < gridDim.x) {
+    if (a.pf_blocks > 0 && threadIdx.x == 0 && (int)blockIdx.x + a.pf_blocks < ncta) {
         const unsigned c = blockIdx.x + a.pf_blocks;
         prefetch_block<T>((const T *)a.fin, a.nbr, a.npad, a.npad,
-                          (long long)a.blk_list[c / H] * H + c % H, BT);
+                          (long long)list[c / H] * H + c % H, BT);
     }
     double sum_u = 0.0, sum_r = 0.0;
     float dmax = 0.f;

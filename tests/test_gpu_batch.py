@@ -92,3 +92,39 @@ def test_batch_convergence_retires_and_backfills():
         assert b.info()["used_nodes"] == 0
         s2 = b.add_packed(13, 16, 16, 16, 2.0, 3.0, 0.5, 0.9, 1e-5, tol=1e-4)
         assert s2 >= 0
+
+
+GROUP_SAMPLES = [((20, 18, 16), 3, 3.0, 4.0, 0.45, 0.8, 2e-4),
+                 ((12, 12, 12), 4, 2.0, 3.0, 0.40, 1.1, 1e-4),
+                 ((40, 36, 32), 6, 3.0, 6.0, 0.40, 0.9, 1e-4),
+                 ((24, 16, 20), 5, 2.5, 5.0, 0.35, 0.65, 5e-5),
+                 ((16, 16, 16), 7, 2.0, 4.0, 0.50, 1.3, 2e-4),
+                 ((28, 28, 28), 8, 3.0, 5.0, 0.30, 0.7, 1e-4)]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16dev", "bf16dev"])
+def test_l2_groups_change_no_bit(precision):
+    """The pool's L2 groups (samples that fit a budget step their interval
+    group by group) against one chain over every sample: the same f and
+    the same results.  A 1 MiB budget makes several groups and leaves the
+    40x36x32 sample outside them; True takes 60% of the L2 (one group)."""
+    K = 20
+    out = {}
+    for groups in (False, 1024, True):
+        with Batch(400000, 16, precision, check_every=K, l2_groups=groups) as b:
+            ids = [b.add_flag(pack_flag(dims, seed, rmin, rmax, phi), *dims, tau, force,
+                              tol=0.0, max_steps=3 * K)
+                   for dims, seed, rmin, rmax, phi, tau, force in GROUP_SAMPLES]
+            b.run(2)
+            fs = [b.get_f(sid) for sid in ids]
+            b.run(3)
+            res = [b.result(sid) for sid in ids]
+            out[groups] = (fs, res)
+    base_f, base_r = out[False]
+    for groups in (1024, True):
+        fs, res = out[groups]
+        for a, c in zip(fs, base_f):
+            assert np.array_equal(a, c), groups
+        for a, c in zip(res, base_r):
+            assert a["k_darcy"] == c["k_darcy"] and a["steps"] == c["steps"], groups
+            assert a["status"] == c["status"] == 2, groups
