@@ -459,11 +459,23 @@ def run_gpu(args, rank, world, local):
         # latency, answers against FP64) and the batched pool against the
         # plain kernel; bounded runs of the serving and batched workloads
         t0 = time.perf_counter()
-        line["served"] = served_result(args.extra_requests, args.extra_rate,
-                                       args.budget_gb, args.serve_precision,
-                                       args.serve_check_every, args.max_steps,
-                                       max_wall=args.extra_wall, fp64_check=0,
-                                       plain_fp64=True)
+        served = served_result(args.extra_requests, args.extra_rate,
+                               args.budget_gb, args.serve_precision,
+                               args.serve_check_every, args.max_steps,
+                               max_wall=args.extra_wall, fp64_check=0,
+                               plain_fp64=True)
+        ks64 = served.pop("_plain_ks")
+        line["served"] = served
+        # the serving configuration as specified: FP16 deviation storage
+        # (with the hand-off to FP32 that lets tight tolerances finish), on
+        # the same requests, answers against the same FP64 plain solves
+        if args.serve_precision != "fp16dev":
+            c5 = served_result(args.extra_requests, args.extra_rate,
+                               args.budget_gb, "fp16dev", args.serve_check_every,
+                               args.max_steps, max_wall=args.extra_wall,
+                               fp64_check=0, plain_ks=ks64)
+            c5.pop("_plain_ks")
+            line["served_fp16"] = c5
         line["batched"] = batched_result(args.samples, args.check_every,
                                          args.max_steps, args.plain_steps)
         line["extras_wall_s"] = round(time.perf_counter() - t0, 1)
@@ -668,13 +680,16 @@ SERVE_FORMS = {"fp16dev": "FP16 deviations", "bf16dev": "BF16 deviations",
 
 
 def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
-                  max_wall=None, fp64_check=32, plain_fp64=False):
+                  max_wall=None, fp64_check=32, plain_fp64=False, plain_ks=None):
     """The serving workload (n_requests Poisson requests of seed 4 at `rate`
     per second) through the continuous-batching server, with the
     permeabilities checked against FP64: a pooled FP64 solve of the first
     fp64_check answered requests, and with plain_fp64 the FP64 plain form
     serving every answered request one at a time (first come first
-    served), which also gives that form's solves/s and latencies."""
+    served), which also gives that form's solves/s and latencies.  plain_ks
+    (request index -> k of the FP64 plain form, from an earlier run on the
+    same requests) compares the answers without solving them again.  The
+    result's "_plain_ks" holds the FP64 plain form's k per request."""
     from porelb_gb300.serve import Server
     from porelb_gb300.workloads import serving_requests
     reqs = serving_requests(n_requests, 4, rate)
@@ -688,6 +703,7 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
     errs = [abs(by[i]["k_darcy"] - r["k_darcy"]) / abs(r["k_darcy"])
             for i, r in res64.items() if r["k_darcy"]]
     plain = None
+    ks64 = dict(plain_ks or {})
     if plain_fp64:
         served = [r for r in reqs if r.index in by]
         ks64, plain = _plain_fp64_fcfs(served, K, max_steps)
@@ -699,6 +715,7 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
             "max": max(perr) if perr else None,
             "median": statistics.median(perr) if perr else None,
             "within_1e-3": sum(e <= 1e-3 for e in perr), "of": len(perr)}
+    aerr = [abs(by[i]["k_darcy"] - k) / abs(k) for i, k in ks64.items() if k and i in by]
     return {
         "metric": "perm solves/s (served, %s)" % SERVE_FORMS[precision],
         "value": round(summ["solves_per_s"], 3), "unit": "solves/s",
@@ -715,6 +732,11 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
                               "within_1e-3": sum(e <= 1e-3 for e in errs)},
         "fp64_mlups_on_checked": round(ns64 / wall64 / 1e6, 1) if wall64 else None,
         "plain_fp64_fcfs": plain,
+        # every answer against the FP64 plain form's k of the same request
+        "k_rel_err_vs_plain_fp64": ({"max": max(aerr), "median": statistics.median(aerr),
+                                     "within_1e-3": sum(e <= 1e-3 for e in aerr),
+                                     "of": len(aerr)} if aerr else None),
+        "_plain_ks": ks64,
         "time_split_s": {"admission_overlapped": round(summ["admit_s"], 2),
                          "waiting_for_intervals": round(summ["wait_s"], 2),
                          "gpu_busy": round(summ["gpu_busy_s"], 2),
@@ -733,10 +755,12 @@ def served_result(n_requests, rate, budget_gb, precision, K, max_steps,
 def run_served(args):
     import torch
     torch.cuda.set_device(0)
-    print(json.dumps(served_result(args.requests, args.rate, args.budget_gb,
-                                   args.serve_precision, args.serve_check_every,
-                                   args.max_steps, args.max_wall, args.fp64_check,
-                                   args.plain_fp64)), flush=True)
+    res = served_result(args.requests, args.rate, args.budget_gb,
+                        args.serve_precision, args.serve_check_every,
+                        args.max_steps, args.max_wall, args.fp64_check,
+                        args.plain_fp64)
+    res.pop("_plain_ks")
+    print(json.dumps(res), flush=True)
 
 
 def _steady_flag(flag, dims, precision, tau, force, tol, K, max_steps):
