@@ -250,9 +250,12 @@ int plb_last_error(plb_sim *sim, int *it, int *node, int *x, int *y, int *z,
                    double *rho);
 
 /* What the step kernel reported since plb_init_equilibrium, read at each
- * synchronising call: PLB_FLAG_FX_FALLBACK when the fixed-point FP64 form
- * met a node whose populations left its range and recomputed that node in
- * native FP64.  No reference counterpart (the reference has one form). */
+ * synchronising call: PLB_FLAG_FX_FALLBACK when a node's populations left
+ * the range of the form's fast arithmetic and the node was recomputed with
+ * native FP64 operations (the fixed-point form: populations far from the
+ * weights; the bit-exact form: values or a density outside [2^-64, 2^64),
+ * exact zeros included).  Results keep the form's accuracy either way.  No
+ * reference counterpart (the reference has one form). */
 #define PLB_FLAG_FX_FALLBACK 2u
 int plb_kernel_flags(plb_sim *sim, unsigned *flags);
 

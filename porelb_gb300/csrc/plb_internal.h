@@ -76,6 +76,9 @@ struct Coeffs {
     float scale, inv_scale; /* deviation storage scale */
     fx::Consts fxk;         /* fixed-point form */
     int it;                 /* iteration number (the it > 0 rule) */
+    /* bit-exact form: a run constant outside the range of the integer
+     * multiply's node check (every node then takes the native multiply) */
+    int exact_native;
 };
 
 struct StepArgs {

@@ -17,6 +17,7 @@
 
 #include <atomic>
 
+#include "plb_emu.h"
 #include "plb_internal.h"
 
 using namespace plb;
@@ -228,6 +229,12 @@ void make_coeffs(double tau, double force, float scale, Coeffs *c)
     c->scale = scale;
     c->inv_scale = 1.0f / scale;
     c->fxk = fx::make_consts(tau, force);
+    const double consts[5] = {c->omega, c->om1, c->k3, c->force, c->half_force};
+    for (double x : consts) {
+        uint64_t b;
+        memcpy(&b, &x, 8);
+        c->exact_native |= (int)emu::outside_node_range(b);
+    }
 }
 
 int scan_words(const uint32_t *cnt, uint32_t *offs, size_t m, cudaStream_t st)

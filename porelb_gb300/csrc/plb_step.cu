@@ -41,13 +41,20 @@ __device__ __forceinline__ float w32(int c)
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-/* the same product on the integer pipes (plb_emu.h): the same bits.  The
- * bit-exact collision sends 84 of its 97 products per node here, which
- * balances the FP64 and integer pipes (2.05 -> 2.68 GLUPS at 256^3). */
+/* the same product on the integer pipes (plb_emu.h): the same bits for a
+ * node whose values, density and run constants passed the range check.
+ * The bit-exact collision sends 84 of its 97 products per node here, which
+ * balances the FP64 and integer pipes (2.05 -> 2.68 GLUPS at 256^3); a
+ * node outside the range takes the NATIVE products. */
+template <bool NATIVE>
 __device__ __forceinline__ double imul(double a, double b)
 {
-    return __longlong_as_double((long long)emu::dmul_bits(
-        (uint64_t)__double_as_longlong(a), (uint64_t)__double_as_longlong(b)));
+    if constexpr (NATIVE) {
+        return __dmul_rn(a, b);
+    } else {
+        return __longlong_as_double((long long)emu::dmul_bits_fast(
+            (uint64_t)__double_as_longlong(a), (uint64_t)__double_as_longlong(b)));
+    }
 }
 
 /* ------------------------------------------------------------- gather */
@@ -116,8 +123,9 @@ struct Macro {
     bool bad;
 };
 
+template <bool NATIVE>
 __device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
-                                                     const Coeffs &a)
+                                                     const Coeffs &a, uint32_t &outside)
 {
     Macro m;
     double rho = f[0];
@@ -127,6 +135,13 @@ __device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
     const double rv = moment_ref<1>(f);
     const double rw = moment_ref<2>(f);
     m.bad = (rho > 1.2) | (rho < 0.5);
+    if constexpr (!NATIVE) {
+        /* the density in [2^-64, 2^64) too, or the node takes the native
+         * multiply (the caller) */
+        const uint64_t rb = (uint64_t)__double_as_longlong(rho);
+        outside |= emu::outside_node_range(rb) | (uint32_t)((rb << 1) == 0ull);
+        if (outside) return m;
+    }
     if (a.it > 0) ru = dadd(ru, a.half_force);
     const double u = __ddiv_rn(ru, rho);
     const double v = __ddiv_rn(rv, rho);
@@ -145,8 +160,8 @@ __device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
 
     /* rest direction: e.u = 0 gives ((1 + 0) + 0) - 1.5 uv */
     {
-        const double feq = imul(h0, dsub(1.0, uv15));
-        f[0] = dadd(imul(a.om1, f[0]), imul(a0, feq));
+        const double feq = imul<NATIVE>(h0, dsub(1.0, uv15));
+        f[0] = dadd(imul<NATIVE>(a.om1, f[0]), imul<NATIVE>(a0, feq));
     }
     /* pairs (J, J+1) with e_{J+1} = -e_J: 3 e.u, 4.5 e.u and (4.5 e.u) e.u
      * of the partner are exact negations / the same value. */
@@ -162,15 +177,15 @@ __device__ __forceinline__ Macro collide_fp64_exact(double (&f)[Q],
                         : (J == 13) ? eu_ref<13>(u, v, w)
                         : (J == 15) ? eu_ref<15>(u, v, w)
                                     : eu_ref<17>(u, v, w);
-        const double t3 = imul(3.0, eu);
-        const double c2 = imul(imul(4.5, eu), eu);
+        const double t3 = imul<NATIVE>(3.0, eu);
+        const double c2 = imul<NATIVE>(imul<NATIVE>(4.5, eu), eu);
         const double h = wclass(J) == 1 ? h1 : h2;
-        const double feqJ = imul(h, dsub(dadd(dadd(1.0, t3), c2), uv15));
-        const double feqK = imul(h, dsub(dadd(dsub(1.0, t3), c2), uv15));
+        const double feqJ = imul<NATIVE>(h, dsub(dadd(dadd(1.0, t3), c2), uv15));
+        const double feqK = imul<NATIVE>(h, dsub(dadd(dsub(1.0, t3), c2), uv15));
         const double AJ = ex(J) > 0 ? ap : (ex(J) < 0 ? am : a0);
         const double AK = ex(K) > 0 ? ap : (ex(K) < 0 ? am : a0);
-        f[J] = dadd(imul(a.om1, f[J]), imul(AJ, feqJ));
-        f[K] = dadd(imul(a.om1, f[K]), imul(AK, feqK));
+        f[J] = dadd(imul<NATIVE>(a.om1, f[J]), imul<NATIVE>(AJ, feqJ));
+        f[K] = dadd(imul<NATIVE>(a.om1, f[K]), imul<NATIVE>(AK, feqK));
     }
     return m;
 }
@@ -346,6 +361,25 @@ template <int PREC, int V> struct MinBlocks {
 
 /* Gather, collide and store node i.  Returns the macros; *dev_max receives
  * the largest stored deviation magnitude of the 16-bit forms. */
+/* The bit-exact collision of node i with every product on the FP64 pipe,
+ * from its streamed values gathered again, stored: the path of a node
+ * whose values or density (or the run's constants) lie outside the range
+ * of the integer multiply's check, such as an infinity, a NaN, a subnormal
+ * or an extreme value.  Out of line, so the common path keeps its
+ * registers. */
+__device__ __noinline__ Macro exact_node_native(const double *fin, double *fout,
+                                                const uint32_t *nbr, long long np,
+                                                long long i, const Coeffs &co)
+{
+    double raw[Q];
+    gather<double>(fin, nbr, np, i, raw);
+    uint32_t unused = 0;
+    const Macro m = collide_fp64_exact<true>(raw, co, unused);
+#pragma unroll
+    for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
+    return m;
+}
+
 /* Collide node i's streamed values raw[] and store them. */
 template <int PREC, bool MACRO, typename T>
 __device__ __forceinline__ Macro collide_node(T (&raw)[Q], const T *fin, T *fout,
@@ -367,8 +401,28 @@ __device__ __forceinline__ Macro collide_node(T (&raw)[Q], const T *fin, T *fout
 #pragma unroll
         for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
     } else if constexpr (PREC == PLB_FP64_EXACT || PREC == PLB_FP64_FMA) {
-        if constexpr (PREC == PLB_FP64_EXACT) m = collide_fp64_exact(raw, co);
-        else m = collide_fp64_fma(raw, co);
+        if constexpr (PREC == PLB_FP64_EXACT) {
+            /* the integer multiply needs the node's values in [2^-64, 2^64)
+             * (and its density, checked in the collision): their smallest
+             * and largest exponent field (a zero value, which the range
+             * admits but a distribution never is, takes the native path) */
+            uint32_t emin = 0x7ffu, emax = 0u;
+#pragma unroll
+            for (int j = 0; j < Q; j++) {
+                const uint32_t e = ((uint32_t)__double2hiint(raw[j]) >> 20) & 0x7ffu;
+                emin = min(emin, e);
+                emax = max(emax, e);
+            }
+            uint32_t outside = (uint32_t)co.exact_native | (uint32_t)(emin < 1023u - 64u) |
+                               (uint32_t)(emax > 1023u + 63u);
+            if (!outside) m = collide_fp64_exact<false>(raw, co, outside);
+            if (outside) {
+                flags |= 2u;
+                return exact_node_native(fin, fout, nbr, np, i, co);
+            }
+        } else {
+            m = collide_fp64_fma(raw, co);
+        }
 #pragma unroll
         for (int j = 0; j < Q; j++) __stcs(fout + (long long)j * np + i, raw[j]);
     } else {

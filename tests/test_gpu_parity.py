@@ -176,6 +176,35 @@ def oracle_pull_from(V, vs, f0, tau, force, it_begin, steps):
     return f0, mac
 
 
+def test_exact_form_native_path_for_out_of_range_nodes():
+    """The bit-exact form multiplies on the integer pipes only for nodes
+    whose values and density lie in [2^-64, 2^64); other nodes (an exact
+    zero, a value of 2^-100, a subnormal value, and the neighbours they
+    stream to) take native multiplies.  The kernel reports it, and the
+    result equals the oracle bit for bit."""
+    dims, tau, force, steps = (20, 18, 16), 0.8, 1e-4, 2
+    flag = pack_flag(dims, 9, 2.5, 4.0, 0.45)
+    V, vs = P.build_table(flag, *dims, 1)
+    N = len(V)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    rng = np.random.default_rng(11)
+    f = np.tile(w, (N, 1)) * (1 + 0.05 * rng.uniform(-1, 1, (N, 19)))
+    nodes = rng.choice(N, 40, replace=False)
+    for q, i in enumerate(nodes):
+        f[i, 1 + q % 18] = (0.0, 2.0 ** -100, 1e-310)[q % 3]
+    ref_f, ref_mac = oracle_pull_from(V, vs, f.reshape(-1), tau, force, 1, steps)
+    with gpu_run(V, dims, vs, tau, force, 0, precision="fp64_exact") as sim:
+        sim.set_f(f.reshape(-1))
+        sim.step(steps, it_begin=1)
+        assert sim.kernel_flags() & 2, "the native path did not run"
+        got = sim.get_f()
+        assert np.array_equal(got.view(np.uint64), ref_f.view(np.uint64))
+        assert np.array_equal(sim.macros().view(np.uint64), ref_mac.view(np.uint64))
+    # a state inside the range keeps the integer path everywhere
+    with gpu_run(V, dims, vs, tau, force, 20, precision="fp64_exact") as sim:
+        assert not sim.kernel_flags() & 2
+
+
 def test_fixed_point_fallback_fires_and_stays_within_1e12():
     """A state whose populations lie far outside the fixed-point form's range
     (deviations up to 60% of the weights at one node in twenty): those
